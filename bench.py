@@ -1,0 +1,372 @@
+#!/usr/bin/env python3
+"""Benchmark of the event-based macroscopic cross-section lookup on GB300.
+
+One step = one pass of the lookup over the whole event batch of the workload
+(default: the large problem on the unionized grid, 17,000,000 lookups, the
+plain kernel).  Prints one JSON line (rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+                    [--kernel plain|batched] [--arith fast|exact]
+    python bench.py --impl reference ...   # the reference's CPU path on the host cores
+
+Timing: W untimed steps, then K steps bracketed by a barrier and
+cudaStreamSynchronize, timed with CUDA events on the stream the kernels run
+on; the tables (5.7 GB index grid) are larger than L2, so no flush is needed.
+Multi-GPU: one process per GPU; rank r takes event indices
+[r*N, (r+1)*N) (weak scaling, no data-path collective); value = all ranks'
+lookups / max over ranks of the timed span.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "lookups/s device-timed, large unionized; batched & fwd+adjoint vs plain, FP64"
+UNIT = "lookups/s"
+
+WORKLOADS = {
+    "large_unionized": dict(size="large", grid="unionized"),
+    "large_hash": dict(size="large", grid="hash"),
+    "large_nuclide": dict(size="large", grid="nuclide"),
+    "small_unionized": dict(size="small", grid="unionized"),
+    "xl_hash": dict(size="XL", grid="hash", lookups=100000000),
+    "xl_nuclide": dict(size="XL", grid="nuclide", lookups=100000000),
+}
+# openmp-threading/Simulation.c:433-445
+DIST = [0.140, 0.052, 0.275, 0.134, 0.154, 0.064, 0.066, 0.055, 0.008, 0.015, 0.025, 0.013]
+
+
+def material_probabilities():
+    """P(material) of pick_mat (Simulation.c:447-459): cumulative sums skip dist[0]."""
+    run = [sum(DIST[j] for j in range(i, 0, -1)) for i in range(12)]
+    p = [0.0] * 12
+    prev = 0.0
+    for i in range(1, 12):
+        p[i] = run[i] - prev
+        prev = run[i]
+    p[0] = 1.0 - prev
+    return p
+
+
+def algorithmic_bytes_per_lookup(inputs, num_nucs) -> float:
+    """Bytes one lookup must move from the tables (the reference algorithm):
+    union search 8 B per probe, then per nuclide its index entry and the
+    96-byte pair of bracketing gridpoints (hash: the two bracket energies and
+    the in-bin search; nuclide: the full per-nuclide search)."""
+    nbar = sum(p * n for p, n in zip(material_probabilities(), num_nucs))
+    n_gp = inputs.n_gridpoints
+    if inputs.grid_type == 0:
+        n_union = inputs.n_isotopes * n_gp
+        return 8 * math.ceil(math.log2(n_union)) + nbar * (4 + 96)
+    if inputs.grid_type == 2:
+        probes = math.ceil(math.log2(n_gp / inputs.hash_bins + 2))
+        return nbar * (8 + 16 + 8 * probes + 96)
+    return nbar * (8 * math.ceil(math.log2(n_gp)) + 96)
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(workload, kernel):
+    """dram read+write bytes per lookup of the dominant kernel, from the ncu
+    summary committed under profiles/ (line 'dram_bytes_per_lookup: X')."""
+    name = os.path.join(ROOT, "profiles", f"{'k_plain' if kernel == 'plain' else 'k_batched_lookup'}_{workload}.md")
+    try:
+        for line in open(name):
+            if line.strip().startswith("dram_bytes_per_lookup:"):
+                return float(line.split(":", 1)[1].split()[0]), os.path.relpath(name, ROOT)
+    except OSError:
+        pass
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline_oracle(inputs_x, problem, workload, budget_s=10.0):
+    """The oracle port timed on this host's cores over a bounded sample of the
+    same workload, reusing the (bit-identical) setup arrays."""
+    import oracle
+    L = oracle.lib()
+    oin = oracle.Inputs()
+    C.memmove(C.byref(oin), C.byref(inputs_x), C.sizeof(oin))
+    sd = C.cast(C.byref(problem.sd), C.POINTER(oracle.SimData))
+    cores = os.cpu_count() or 1
+    n = 200000
+    t0 = time.perf_counter()
+    L.or_run_event(C.byref(oin), sd, 0, n, cores, None, None, None, None)
+    dt = time.perf_counter() - t0
+    n2 = int(min(inputs_x.lookups, max(n, n * budget_s / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    L.or_run_event(C.byref(oin), sd, 0, n2, cores, None, None, None, None)
+    dt2 = time.perf_counter() - t0
+    return {"value": n2 / dt2, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"lookups [0, {n2}) of {workload} ({n2 / inputs_x.lookups:.1%} of the batch), "
+                      f"{dt2:.2f} s on {cores} threads"}
+
+
+# ------------------------------------------------------------- reference arm
+def reference_arm(args, rank):
+    """The reference's own CPU implementation of the path on the host cores:
+    the reference library built from its sources (oracle/_ref) where it was
+    built for this machine, else the oracle port of it."""
+    if rank != 0:
+        return 0
+    import oracle
+    wl = WORKLOADS[args.workload]
+    cfg = oracle.Config(size=wl["size"], grid=wl["grid"], lookups=wl.get("lookups"))
+    inp = cfg.inputs()
+    cores = os.cpu_count() or 1
+    kind = "port"
+    ref = None
+    if os.path.exists(oracle.REF_LIB_PATH):
+        try:
+            ref = C.CDLL(oracle.REF_LIB_PATH)
+            ref.refh_grid_init.restype = C.POINTER(oracle.SimData)
+            ref.refh_grid_init.argtypes = [C.POINTER(oracle.Inputs)]
+            ref.refh_run_event.restype = C.c_ulonglong
+            ref.refh_run_event.argtypes = [C.POINTER(oracle.Inputs), C.POINTER(oracle.SimData),
+                                           C.c_long, C.c_long] + [C.c_void_p] * 4
+            ref.refh_set_threads.argtypes = [C.c_int]
+            ref.refh_set_threads(cores)
+            kind = "reference"
+        except OSError:
+            ref = None
+    if ref is not None:
+        sdp = ref.refh_grid_init(C.byref(inp))
+        run = lambda a, n: ref.refh_run_event(C.byref(inp), sdp, a, n, None, None, None, None)  # noqa: E731
+    else:
+        prob = oracle.Problem(cfg)
+        L = oracle.lib()
+        run = lambda a, n: L.or_run_event(C.byref(prob.inp), C.byref(prob.sd), a, n, cores,  # noqa: E731
+                                          None, None, None, None)
+    # a bounded sample per step: about 2 s of work at the measured rate
+    t0 = time.perf_counter()
+    run(0, 100000)
+    rate0 = 100000 / (time.perf_counter() - t0)
+    per_step = int(min(inp.lookups // max(1, args.steps), max(100000, rate0 * 2.0)))
+    for s in range(args.warmup):
+        run(s * per_step % max(1, inp.lookups - per_step), per_step)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        run((s * per_step) % max(1, inp.lookups - per_step), per_step)
+    t = time.perf_counter() - t0
+    value = per_step * args.steps / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (the reference's LCG generators)",
+        "config": {"workload": args.workload, "kernel": "openmp-threading event loop (k0)",
+                   "sample_lookups_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{per_step} consecutive lookups of {args.workload} per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- our arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large_unionized", choices=sorted(WORKLOADS))
+    ap.add_argument("--kernel", default="plain", choices=["plain", "batched"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+
+    import torch
+    import xsbench_gb300 as X
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    wl = dict(WORKLOADS[args.workload])
+    inputs = X.make_inputs(method="event", **wl)
+    N = inputs.lookups
+    t_setup = time.perf_counter()
+    problem = X.grid_init(inputs)
+    ctx = X.Context(inputs, problem, device=local)
+    t_setup = time.perf_counter() - t_setup
+    first = rank * N
+    stream = torch.cuda.current_stream()
+    kw = dict(kernel=args.kernel, arith=args.arith, first=first, count=N, stream=stream)
+
+    # correctness of this very configuration (rank 0 holds lookups [0, N))
+    r = ctx.run_event(**kw)
+    expected = X.EXPECTED_HASH.get(("event", wl["size"].lower()))
+    hash_ok = (expected is None or rank != 0 or N != 17000000 or r.hash == expected)
+    for _ in range(args.warmup):
+        ctx.run_event(async_=True, **kw)
+    ctx.sync()
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        launches += ctx.run_event(async_=True, **kw).kernel_launches
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    last = ctx.sync()
+    if dist:
+        dist.barrier()
+    t = ev0.elapsed_time(ev1) / 1e3
+    t_max = t
+    if dist:
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * N * args.steps / t_max
+    hash_ok = hash_ok and (rank != 0 or expected is None or N != 17000000
+                           or last.hash == expected)
+
+    # end to end through the C ABI with host buffers: samples in, macro_xs out
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    hE, hM = pin((N,), torch.float64), pin((N,), torch.int32)
+    ctx.sample_event(first, N, hE, hM)
+    hmacro, hidx = pin((N, 5), torch.float64), pin((N,), torch.uint8)
+    ekw = dict(kernel=args.kernel, arith=args.arith)
+    ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)  # warm
+    e2e_t = []
+    for _ in range(max(1, args.e2e_steps)):
+        t0 = time.perf_counter()
+        re = ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ok = re.verification == last.verification
+    e2e_value = world * N / statistics.median(e2e_t)
+
+    line = None
+    if rank == 0:
+        bpl = algorithmic_bytes_per_lookup(inputs, list(problem.arrays()["num_nucs"]))
+        peak, peak_kind = measured_peak_gbs()
+        per_launch_s = t / args.steps
+        achieved = N * bpl / per_launch_s / 1e9
+        traffic_pl, traffic_src = profiled_traffic(args.workload, args.kernel)
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cpu = cpu_baseline_oracle(inputs, problem, args.workload, args.cpu_budget)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the reference's own LCG problem generators)",
+            "config": {"workload": args.workload, "kernel": args.kernel, "arith": args.arith,
+                       "n_isotopes": inputs.n_isotopes, "n_gridpoints": inputs.n_gridpoints,
+                       "grid": wl["grid"], "lookups_per_gpu": N,
+                       "l2": "inputs larger than L2 (tables > 129 MB), no flush",
+                       "parallelism": f"shards x{world} (event index ranges)",
+                       "hash_ok": bool(hash_ok), "hash": last.hash,
+                       "setup_s": round(t_setup, 2)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_lookup": bpl,
+                         "traffic": (traffic_pl * N if traffic_pl else None),
+                         "traffic_source": traffic_src},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 12,
+                    "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",
+                    "verification_matches": bool(e2e_ok)},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    problem.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0 if hash_ok else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,244 @@
+/*
+ * xsgb.h -- C ABI of the GB300 (sm_103a) event-based macroscopic
+ * cross-section lookup: a drop-in for the lookup loop of XSBench.
+ *
+ * Plain C: pointers, sizes and status codes only, so that C, ctypes, cgo or
+ * any other FFI can bind it.  Every call returns an xs_status and never exits
+ * the process; xs_last_error() holds the message of the calling thread's last
+ * failure.  A context (xs_ctx) owns the device copy of one problem; it is not
+ * thread-safe (one context per host thread), and calls on it are ordered on
+ * the context's CUDA stream and block until their results are written.
+ *
+ * The struct layouts xs_gridpoint / xs_inputs / xs_simdata are identical to
+ * NuclideGridPoint / Inputs / SimulationData of the reference
+ * (openmp-threading/XSbench_header.h:54-102, AML members absent), so arrays made
+ * by the reference's grid_init_do_not_profile (openmp-threading/GridInit.c:3)
+ * can be passed by pointer cast, and arrays made by xs_grid_init can be passed
+ * back to the reference's own functions.
+ */
+#ifndef XSGB_H
+#define XSGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XSGB_VERSION 1
+
+/* ------------------------------------------------------------------ types */
+
+typedef enum {
+    XS_OK = 0,
+    XS_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or option (reference: print_CLI_error/exit) */
+    XS_ERR_OUT_OF_MEMORY = 2,    /* host or device allocation failed (reference: assert) */
+    XS_ERR_CUDA = 3,             /* a CUDA runtime call failed (reference: gpuErrchk abort) */
+    XS_ERR_NO_DEVICE = 4,        /* no usable sm_103 device */
+    XS_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out */
+    XS_ERR_DATA = 6,             /* a checked run found an out-of-range table index or material */
+    XS_ERR_UNSUPPORTED = 7,      /* option not available for this problem */
+    XS_ERR_IO = 8                /* file could not be read or written */
+} xs_status;
+
+/* Grid types: openmp-threading/XSbench_header.h:37-39 */
+enum { XS_UNIONIZED = 0, XS_NUCLIDE = 1, XS_HASH = 2 };
+/* Simulation methods: openmp-threading/XSbench_header.h:42-43 */
+enum { XS_HISTORY_BASED = 1, XS_EVENT_BASED = 2 };
+/* Binary modes: openmp-threading/XSbench_header.h:46-48 */
+enum { XS_BINARY_NONE = 0, XS_BINARY_READ = 1, XS_BINARY_WRITE = 2 };
+
+typedef struct { /* = NuclideGridPoint, openmp-threading/XSbench_header.h:54-61 */
+    double energy;
+    double total_xs;
+    double elastic_xs;
+    double absorbtion_xs;
+    double fission_xs;
+    double nu_fission_xs;
+} xs_gridpoint;
+
+typedef struct { /* = Inputs, openmp-threading/XSbench_header.h:63-75 */
+    int nthreads;
+    long n_isotopes;
+    long n_gridpoints;
+    int lookups;
+    char *HM;
+    int grid_type;
+    int hash_bins;
+    int particles;
+    int simulation_method;
+    int binary_mode;
+    int kernel_id;
+} xs_inputs;
+
+typedef struct { /* = SimulationData, openmp-threading/XSbench_header.h:77-102 */
+    int *num_nucs;
+    double *concs;
+    int *mats;
+    double *unionized_energy_array;
+    int *index_grid;
+    xs_gridpoint *nuclide_grid;
+    int length_num_nucs;
+    int length_concs;
+    int length_mats;
+    int length_unionized_energy_array;
+    long length_index_grid;
+    int length_nuclide_grid;
+    int max_num_nucs;
+    double *p_energy_samples;
+    int length_p_energy_samples;
+    int *mat_samples;
+    int length_mat_samples;
+} xs_simdata;
+
+typedef struct xs_ctx xs_ctx;
+
+/* Lookup kernels.  PLAIN is the drop-in for the event loop
+ * (openmp-threading/Simulation.c:15, cuda/Simulation.cu:15): one launch that
+ * samples, block-sorts by material and looks up.  BATCHED is the sorted form
+ * (cuda/Simulation.cu:1024, optimisation 6): on-device counting sort by
+ * (material, energy bucket), then one persistent lookup kernel, all in one
+ * CUDA graph. */
+typedef enum { XS_KERNEL_PLAIN = 0, XS_KERNEL_BATCHED = 1 } xs_kernel;
+
+/* Arithmetic.  EXACT performs the reference's floating-point operations in the
+ * reference's order with no fused multiply-add and IEEE division
+ * (openmp-threading/Simulation.c:307-322, :372-373), so every macro_xs is
+ * bit-identical to the reference's.  FAST interpolates with per-interval slopes
+ * precomputed at context creation (one subtraction and five FMAs per nuclide
+ * instead of a division and fifteen operations); its macro_xs stay within
+ * 1e-12 relative of the reference's.  Both are FP64 throughout. */
+typedef enum { XS_ARITH_FAST = 0, XS_ARITH_EXACT = 1 } xs_arith;
+
+typedef struct {
+    int kernel;          /* xs_kernel */
+    int arith;           /* xs_arith */
+    long first;          /* first event index (lookup i uses seed skip 2*i) */
+    long count;          /* number of lookups; <= 0 means inputs.lookups - first */
+    int block_threads;   /* 0 = tuned default; else 128, 256 or 512 */
+    int tile_lookups;    /* PLAIN: lookups per block tile; 0 = default */
+    int energy_buckets;  /* BATCHED: energy buckets per material (power of 2); 0 = default */
+    int checked;         /* 1: bounds-check every table index and report XS_ERR_DATA */
+    int async;           /* 1: only enqueue (device or NULL outputs); finish with xs_ctx_sync */
+    void *stream;        /* cudaStream_t to order on; NULL = the context's own stream */
+} xs_run_opts;
+
+/* Results of one run.  Output arrays may be NULL, host memory or device
+ * memory; host arrays are filled through a device staging buffer. */
+typedef struct {
+    unsigned long long verification; /* un-modded sum of (argmax+1), Simulation.c:110 */
+    float device_ms;                 /* CUDA-event time of the lookup work on the stream */
+    int kernel_launches;             /* kernels this call launched (graph nodes included) */
+} xs_run_result;
+
+/* -------------------------------------------------------- host-side setup */
+
+/* Reads the reference's command line (openmp-threading/io.c:227-454): flags
+ * -t -g -m -l -h -p -s -G -b -k with the same defaults and resolution.  Returns
+ * XS_ERR_INVALID_ARGUMENT where the reference would print_CLI_error() and exit.
+ * out->HM points into argv or at a static string. */
+xs_status xs_read_cli(int argc, char **argv, xs_inputs *out);
+
+/* Builds the problem exactly as grid_init_do_not_profile does
+ * (openmp-threading/GridInit.c:3-230, Materials.c:7-117): same LCG streams,
+ * orders and tables, bit for bit; multi-threaded on the host.
+ * Arrays are malloc'd; release them with xs_simdata_free. */
+xs_status xs_grid_init(const xs_inputs *in, xs_simdata *out);
+void xs_simdata_free(xs_simdata *sd);
+
+/* Dataset file in the reference's format (openmp-threading/io.c:456-508):
+ * the raw xs_simdata struct, then num_nucs, concs, mats, nuclide_grid,
+ * index_grid, unionized_energy_array. */
+xs_status xs_binary_write(const char *path, const xs_simdata *sd);
+xs_status xs_binary_read(const char *path, xs_simdata *out);
+
+/* ------------------------------------------------------------ device side */
+
+/* Copies one problem to device `device` and builds the device-side derived
+ * tables (slope records, search keys, union-grid bins).  Replaces
+ * move_simulation_data_to_device (cuda/GridInit.cu:4).  The caller keeps
+ * ownership of the host arrays. */
+xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out);
+
+/* Builds the problem directly on the device (the same tables as
+ * xs_grid_init, bit for bit), with no host arrays and no upload. */
+xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs_ctx **out);
+
+/* Copies the context's setup arrays back into host arrays shaped like
+ * xs_grid_init's (for checking); release with xs_simdata_free. */
+xs_status xs_ctx_download(xs_ctx *ctx, xs_simdata *out);
+
+/* Releases the device memory (cuda/GridInit.cu:81 release_device_memory). */
+void xs_ctx_destroy(xs_ctx *ctx);
+
+/* Bytes of device memory the context holds. */
+size_t xs_ctx_device_bytes(const xs_ctx *ctx);
+
+/* Fills opts with defaults (PLAIN, FAST, all lookups, tuned shapes). */
+void xs_run_opts_init(xs_run_opts *opts);
+
+/* Event-based lookups [first, first+count) with in-kernel LCG sampling: the
+ * drop-in for run_event_based_simulation (openmp-threading/Simulation.c:15;
+ * cuda/Simulation.cu:15 and :1024).  macro_xs_out (count*5 doubles) and
+ * max_idx_out (count bytes, argmax 0..4) may be NULL. */
+xs_status xs_run_event(xs_ctx *ctx, const xs_run_opts *opts, double *macro_xs_out,
+                       unsigned char *max_idx_out, xs_run_result *result);
+
+/* The event samples alone: energy and material of lookups [first,
+ * first+count), as the reference's sampling loop / kernel produce them
+ * (openmp-threading/Simulation.c:735-750, cuda/Simulation.cu:441).  Output
+ * arrays may be host or device memory. */
+xs_status xs_sample_event(xs_ctx *ctx, long first, long count, double *energy_out,
+                          int *mat_out);
+
+/* Waits for the work enqueued by async runs and returns the last run's
+ * verification sum and error state (device_ms covers the last run). */
+xs_status xs_ctx_sync(xs_ctx *ctx, xs_run_result *result);
+
+/* Lookups of caller-supplied samples (energy, material) -- the sampling split
+ * of optimisation 1 (openmp-threading/Simulation.c:735-750,
+ * cuda/Simulation.cu:441) with the samples owned by the caller.  Arrays may be
+ * host or device memory; host arrays are streamed through the device in
+ * overlapped chunks.  Materials outside 0..11 give XS_ERR_DATA. */
+xs_status xs_lookup_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
+                            const int *mat, long n, double *macro_xs_out,
+                            unsigned char *max_idx_out, xs_run_result *result);
+
+/* History-based lookups (openmp-threading/Simulation.c:116-238) for particles
+ * [first, first+count) of opts (count <= 0: inputs.particles). */
+xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *result);
+
+/* Adjoint of the lookup.  For upstream gradients gbar (count*5, the
+ * derivative of a scalar loss with respect to each macro_xs of lookups
+ * [first, first+count)) it accumulates
+ *   d_concs  (12*max_num_nucs)            += dL/dconcs
+ *   d_xs     (n_isotopes*n_gridpoints*5)  += dL/d(tabulated xs channels)
+ * and writes d_energy (count) = dL/d(sampled energy).  Any output may be NULL.
+ * The search indices are recomputed, not stored.  The sums are deterministic. */
+xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gbar,
+                         double *d_concs, double *d_xs, double *d_energy,
+                         xs_run_result *result);
+
+/* Times the kernel shapes on this context and keeps the fastest as its
+ * defaults; with cache_path non-NULL the choice is read from / merged into a
+ * JSON cache keyed by (device name, problem). */
+xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best);
+
+/* Full drop-in of the reference seam
+ *   unsigned long long run_event_based_simulation(Inputs, SimulationData, int)
+ * (openmp-threading/XSbench_header.h:117): creates a context on device 0,
+ * runs the plain kernel over in.lookups lookups, destroys the context and
+ * stores the un-modded verification sum. */
+xs_status xs_run_event_based_simulation(xs_inputs in, xs_simdata sd, int mype,
+                                        unsigned long long *verification);
+
+/* ----------------------------------------------------------------- errors */
+
+const char *xs_status_str(xs_status s);
+const char *xs_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XSGB_H */

@@ -1,0 +1,209 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the reference.
+
+Bars (the reference: openmp-threading built from source, tests/golden/):
+  * verification sum and the whole per-lookup argmax vector: bit-exact;
+  * EXACT arithmetic: every macro_xs bit-identical (sha256 of the N x 5 array);
+  * FAST arithmetic: every macro_xs within 1e-12 relative of the reference's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import xsbench_gb300 as X
+from conftest import golden_json, golden_npz, oracle_config, product_inputs, sha
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-12
+_CACHE = {}
+
+
+def ctx_for(name):
+    if name not in _CACHE:
+        for k in list(_CACHE):          # keep one large problem resident at a time
+            if not k.startswith("tiny"):
+                _CACHE.pop(k)[1].close()
+        inp = product_inputs(name)
+        prob = X.grid_init(inp)
+        ctx = X.Context(inp, prob)
+        _CACHE[name] = (prob, ctx)
+    return _CACHE[name][1]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cleanup():
+    yield
+    for prob, ctx in _CACHE.values():
+        ctx.close()
+        prob.close()
+    _CACHE.clear()
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def run(ctx, n, **kw):
+    macro = np.empty((n, 5), np.float64)
+    idx = np.empty(n, np.uint8)
+    r = ctx.run_event(macro_out=macro, max_idx_out=idx, **kw)
+    return r, macro, idx
+
+
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "tiny_nuclide"])
+@pytest.mark.parametrize("kernel", ["plain", "batched"])
+@pytest.mark.parametrize("arith", ["exact", "fast"])
+def test_tiny_against_reference(name, kernel, arith):
+    g = golden_json("full_" + name)
+    ctx = ctx_for(name)
+    r, macro, idx = run(ctx, g["lookups"], kernel=kernel, arith=arith)
+    assert r.verification == g["verification"]
+    assert sha(idx) == g["sha256_max_idx"]
+    if arith == "exact":
+        assert sha(macro) == g["sha256_macro_xs"]
+    else:
+        with oracle.Problem(oracle_config(name)) as o:
+            ref = o.run_event(want_macro=True)["macro"]
+        assert rel_err(macro, ref) <= REL_TOL
+
+
+@pytest.mark.parametrize("name", ["small_unionized", "small_hash", "small_nuclide",
+                                  "large_unionized", "large_hash", "large_nuclide"])
+def test_full_size_against_reference(name):
+    g = golden_json("full_" + name)
+    gl = golden_npz("lookups_" + name)
+    ctx = ctx_for(name)
+    n = g["lookups"]
+    r_exact, m_exact, i_exact = run(ctx, n, kernel="plain", arith="exact")
+    assert r_exact.verification == g["verification"]
+    assert r_exact.hash == g["hash"]
+    assert sha(i_exact) == g["sha256_max_idx"]
+    assert sha(m_exact) == g["sha256_macro_xs"]
+    assert np.array_equal(m_exact[gl["index"]], gl["macro_xs"])
+    for kernel in ("plain", "batched"):
+        r, m, i = run(ctx, n, kernel=kernel, arith="fast")
+        assert r.verification == g["verification"], kernel
+        assert sha(i) == g["sha256_max_idx"], kernel
+        assert rel_err(m, m_exact) <= REL_TOL, kernel
+        del m
+    r, _, i = run(ctx, n, kernel="batched", arith="exact")
+    assert r.verification == g["verification"]
+
+
+def test_verification_only_runs_match():
+    g = golden_json("full_tiny_hash")
+    ctx = ctx_for("tiny_hash")
+    for kernel in ("plain", "batched"):
+        for tile, buckets in ((256, 1), (1024, 256), (4096, 65536)):
+            r = ctx.run_event(kernel=kernel, tile=tile, buckets=buckets)
+            assert r.verification == g["verification"], (kernel, tile, buckets)
+            assert r.kernel_launches >= 1
+
+
+def test_shards_add_up():
+    g = golden_json("full_tiny_unionized")
+    ctx = ctx_for("tiny_unionized")
+    n = g["lookups"]
+    cuts = [0, 1, 777, 65536, 131071, n]
+    total = 0
+    parts = []
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        r, _, idx = run(ctx, b - a, first=a, count=b - a, kernel="plain", arith="exact")
+        total += r.verification
+        parts.append(idx)
+    assert total == g["verification"]
+    assert sha(np.concatenate(parts)) == g["sha256_max_idx"]
+
+
+@pytest.mark.parametrize("kernel", ["plain", "batched"])
+def test_caller_samples_host_and_device(kernel):
+    import torch
+    name = "tiny_nuclide"
+    g = golden_json("full_" + name)
+    ctx = ctx_for(name)
+    with oracle.Problem(oracle_config(name)) as o:
+        s = o.run_event(want_samples=True, want_macro=True)
+    E, M = s["energy"], s["mat"]
+    n = E.shape[0]
+    macro = np.empty((n, 5))
+    idx = np.empty(n, np.uint8)
+    r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel=kernel, arith="exact")
+    assert r.verification == g["verification"]
+    assert sha(macro) == g["sha256_macro_xs"]
+    dE = torch.from_numpy(E).cuda()
+    dM = torch.from_numpy(M).cuda()
+    dmacro = torch.empty((n, 5), dtype=torch.float64, device="cuda")
+    didx = torch.empty(n, dtype=torch.uint8, device="cuda")
+    r2 = ctx.lookup_samples(dE, dM, macro_out=dmacro, max_idx_out=didx, kernel=kernel,
+                            arith="exact")
+    torch.cuda.synchronize()
+    assert r2.verification == g["verification"]
+    assert sha(dmacro.cpu().numpy()) == g["sha256_macro_xs"]
+    assert sha(didx.cpu().numpy()) == g["sha256_max_idx"]
+
+
+def test_async_runs_then_sync():
+    import torch
+    g = golden_json("full_tiny_hash")
+    ctx = ctx_for("tiny_hash")
+    n = g["lookups"]
+    out = torch.empty((n, 5), dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        ctx.run_event(macro_out=out, async_=True, stream=s, arith="exact")
+    r = ctx.sync()
+    assert r.verification == g["verification"]
+    torch.cuda.synchronize()
+    assert sha(out.cpu().numpy()) == g["sha256_macro_xs"]
+
+
+def test_history_small_particles():
+    g = golden_json("history_small")
+    inp = X.make_inputs(size="small", grid="unionized", method="history", lookups=34,
+                        particles=2000)
+    with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
+        for arith in ("exact", "fast"):
+            r = ctx.run_history(arith=arith)
+            assert r.verification == g["particles_2000_verification"], arith
+
+
+def test_drop_in_seam():
+    g = golden_json("full_tiny_unionized")
+    inp = product_inputs("tiny_unionized")
+    with X.grid_init(inp) as p:
+        assert X.run_event_based_simulation(inp, p) == g["verification"]
+
+
+def test_bad_material_sample_is_reported():
+    ctx = ctx_for("tiny_hash")
+    E = np.full(1000, 0.5)
+    M = np.zeros(1000, np.int32)
+    M[517] = 12
+    for kernel in ("plain", "batched"):
+        with pytest.raises(X.XSError) as e:
+            ctx.lookup_samples(E, M, kernel=kernel)
+        assert e.value.status == 6
+    # the context stays usable
+    assert ctx.lookup_samples(E, np.zeros(1000, np.int32)).verification > 0
+
+
+def test_corrupt_index_grid_is_rejected():
+    inp = product_inputs("tiny_hash")
+    with X.grid_init(inp) as p:
+        p.sd.index_grid[12345] = 999999          # beyond the nuclide grid
+        with pytest.raises(X.XSError) as e:
+            X.Context(inp, p)
+        assert e.value.status == 6
+        p.sd.mats[3] = 68                        # nuclide id beyond n_isotopes
+        p.sd.index_grid[12345] = 0
+        with pytest.raises(X.XSError) as e:
+            X.Context(inp, p)
+        assert e.value.status == 6
+
+
+def test_checked_runs_pass_on_valid_tables():
+    for name in ("tiny_unionized", "tiny_hash", "tiny_nuclide"):
+        g = golden_json("full_" + name)
+        ctx = ctx_for(name)
+        for kernel in ("plain", "batched"):
+            assert ctx.run_event(kernel=kernel, checked=True).verification == g["verification"]

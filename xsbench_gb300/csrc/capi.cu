@@ -1,0 +1,606 @@
+// capi.cu -- the extern "C" entry points of include/xsgb.h: contexts,
+// runs, the caller-sample pipeline, and error reporting.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "device_common.cuh"
+
+namespace xsgb {
+
+static thread_local std::string g_last_error;
+
+xs_status fail(xs_status s, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+xs_status cuda_fail(cudaError_t e, const char *what)
+{
+    cudaGetLastError();  // clear a sticky launch error where it is not fatal
+    if (e == cudaErrorMemoryAllocation)
+        return fail(XS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(XS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+xs_status ctx_alloc(xs_ctx *ctx, void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(XS_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed (%s)", bytes,
+                    cudaGetErrorString(e));
+    }
+    ctx->allocations.push_back(*p);
+    ctx->device_bytes += bytes;
+    return XS_OK;
+}
+
+template <typename T>
+static xs_status upload(xs_ctx *ctx, const T *host, size_t n, const T **dev)
+{
+    void *p = nullptr;
+    xs_status s = ctx_alloc(ctx, &p, n * sizeof(T));
+    if (s != XS_OK) return s;
+    if (n) XS_CUDA(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    *dev = (const T *)p;
+    return XS_OK;
+}
+
+static bool is_device_pointer(const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static xs_status ensure_stage(xs_ctx *ctx, size_t bytes)
+{
+    if (ctx->s.stage_bytes >= bytes) return XS_OK;
+    if (ctx->s.stage) {
+        cudaFree(ctx->s.stage);
+        ctx->device_bytes -= ctx->s.stage_bytes;
+        ctx->s.stage = nullptr;
+        ctx->s.stage_bytes = 0;
+        for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+        ctx->graphs.clear();
+    }
+    cudaError_t e = cudaMalloc(&ctx->s.stage, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(XS_ERR_OUT_OF_MEMORY, "staging buffer of %zu bytes", bytes);
+    }
+    ctx->s.stage_bytes = bytes;
+    ctx->device_bytes += bytes;
+    return XS_OK;
+}
+
+static xs_status resolve(const xs_ctx *ctx, const xs_run_opts *o, long total, xs_run_opts *r)
+{
+    xs_run_opts_init(r);
+    if (o) *r = *o;
+    if (r->kernel != XS_KERNEL_PLAIN && r->kernel != XS_KERNEL_BATCHED)
+        return fail(XS_ERR_INVALID_ARGUMENT, "unknown kernel %d", r->kernel);
+    if (r->arith != XS_ARITH_FAST && r->arith != XS_ARITH_EXACT)
+        return fail(XS_ERR_INVALID_ARGUMENT, "unknown arithmetic %d", r->arith);
+    if (r->first < 0) return fail(XS_ERR_INVALID_ARGUMENT, "first %ld < 0", r->first);
+    if (r->count <= 0) r->count = total - r->first;
+    if (r->count <= 0) return fail(XS_ERR_INVALID_ARGUMENT, "no lookups in range");
+    if (r->tile_lookups <= 0) r->tile_lookups = ctx->plain_tile;
+    if (r->energy_buckets <= 0) r->energy_buckets = ctx->batched_buckets;
+    if (r->block_threads != 0 && r->block_threads != 256)
+        return fail(XS_ERR_INVALID_ARGUMENT, "block_threads %d: the lookup kernels run 256 threads per block", r->block_threads);
+    return XS_OK;
+}
+
+static xs_status read_back(xs_ctx *ctx, cudaStream_t st, xs_run_result *res)
+{
+    unsigned long long *h = (unsigned long long *)ctx->h_result;
+    XS_CUDA(cudaMemcpyAsync(h, ctx->s.verification, 8, cudaMemcpyDeviceToHost, st));
+    XS_CUDA(cudaMemcpyAsync(h + 1, ctx->s.error, 16, cudaMemcpyDeviceToHost, st));
+    XS_CUDA(cudaStreamSynchronize(st));
+    const int *err = (const int *)(h + 1);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0.f;
+    }
+    if (res) {
+        res->verification = h[0];
+        res->device_ms = ms;
+    }
+    if (err[0])
+        return fail((xs_status)err[0], "device check failed: entry %d, value %d", err[1], err[2]);
+    return XS_OK;
+}
+
+}  // namespace xsgb
+
+using namespace xsgb;
+
+extern "C" {
+
+const char *xs_status_str(xs_status s)
+{
+    switch (s) {
+    case XS_OK: return "ok";
+    case XS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case XS_ERR_OUT_OF_MEMORY: return "out of memory";
+    case XS_ERR_CUDA: return "CUDA error";
+    case XS_ERR_NO_DEVICE: return "no usable device";
+    case XS_ERR_TIMEOUT: return "device wait timed out";
+    case XS_ERR_DATA: return "table or sample out of range";
+    case XS_ERR_UNSUPPORTED: return "unsupported";
+    case XS_ERR_IO: return "I/O error";
+    }
+    return "unknown status";
+}
+
+const char *xs_last_error(void) { return g_last_error.c_str(); }
+
+void xs_run_opts_init(xs_run_opts *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->kernel = XS_KERNEL_PLAIN;
+    o->arith = XS_ARITH_FAST;
+}
+
+size_t xs_ctx_device_bytes(const xs_ctx *ctx) { return ctx ? ctx->device_bytes : 0; }
+
+void xs_ctx_destroy(xs_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+    for (void *p : ctx->allocations) cudaFree(p);
+    if (ctx->s.sort_buf) cudaFree(ctx->s.sort_buf);
+    if (ctx->s.stage) cudaFree(ctx->s.stage);
+    if (ctx->pipe_buf) cudaFree(ctx->pipe_buf);
+    if (ctx->h_result) cudaFreeHost(ctx->h_result);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (int i = 0; i < 2; i++) {
+        if (ctx->pipe_stream[i]) cudaStreamDestroy(ctx->pipe_stream[i]);
+        if (ctx->pipe_event[i]) cudaEventDestroy(ctx->pipe_event[i]);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+static xs_status check_problem(const xs_inputs *in, const xs_simdata *sd)
+{
+    if (!in || !sd) return fail(XS_ERR_INVALID_ARGUMENT, "NULL inputs or simulation data");
+    if (in->n_isotopes < 1 || in->n_gridpoints < 2)
+        return fail(XS_ERR_INVALID_ARGUMENT, "need n_isotopes >= 1 and n_gridpoints >= 2");
+    if (in->grid_type < 0 || in->grid_type > 2) return fail(XS_ERR_INVALID_ARGUMENT, "grid_type %d", in->grid_type);
+    const long n_pts = in->n_isotopes * in->n_gridpoints;
+    if (!sd->nuclide_grid || sd->length_nuclide_grid != n_pts)
+        return fail(XS_ERR_INVALID_ARGUMENT, "nuclide grid length %d, expected %ld", sd->length_nuclide_grid, n_pts);
+    if (!sd->num_nucs || !sd->mats || !sd->concs || sd->length_num_nucs != kMaterials || sd->max_num_nucs < 1 ||
+        sd->length_mats != kMaterials * sd->max_num_nucs || sd->length_concs != sd->length_mats)
+        return fail(XS_ERR_INVALID_ARGUMENT, "material tables malformed");
+    for (int m = 0; m < kMaterials; m++) {
+        if (sd->num_nucs[m] < 0 || sd->num_nucs[m] > sd->max_num_nucs)
+            return fail(XS_ERR_DATA, "num_nucs[%d] = %d outside 0..%d", m, sd->num_nucs[m], sd->max_num_nucs);
+        for (int j = 0; j < sd->num_nucs[m]; j++) {
+            const int nuc = sd->mats[m * sd->max_num_nucs + j];
+            if (nuc < 0 || nuc >= in->n_isotopes)
+                return fail(XS_ERR_DATA, "mats[%d][%d] = %d outside 0..%ld", m, j, nuc, in->n_isotopes - 1);
+        }
+    }
+    if (in->grid_type == XS_UNIONIZED) {
+        if (!sd->unionized_energy_array || !sd->index_grid || sd->length_unionized_energy_array < 2 ||
+            sd->length_index_grid != (long)sd->length_unionized_energy_array * in->n_isotopes)
+            return fail(XS_ERR_INVALID_ARGUMENT, "unionized grid malformed");
+        if (sd->length_unionized_energy_array > 0x7FFFFFFFL)
+            return fail(XS_ERR_INVALID_ARGUMENT, "unionized grid too long");
+    }
+    if (in->grid_type == XS_HASH) {
+        if (in->hash_bins < 1 || !sd->index_grid || sd->length_index_grid != (long)in->hash_bins * in->n_isotopes)
+            return fail(XS_ERR_INVALID_ARGUMENT, "hash grid malformed");
+    }
+    return XS_OK;
+}
+
+static xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
+{
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(XS_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return fail(XS_ERR_NO_DEVICE, "device %d of %d", device, ndev);
+    cudaDeviceProp prop;
+    XS_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(XS_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", device, prop.major, prop.minor);
+    XS_CUDA(cudaSetDevice(device));
+    xs_ctx *ctx = new xs_ctx();
+    ctx->device = device;
+    ctx->inputs = *in;
+    ctx->hm = in->HM ? in->HM : "";
+    ctx->inputs.HM = (char *)ctx->hm.c_str();
+    ctx->sm_count = prop.multiProcessorCount;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaStreamCreateWithFlags(&ctx->pipe_stream[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->pipe_event[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_result, 64);
+    if (e != cudaSuccess) {
+        xs_ctx_destroy(ctx);
+        return cuda_fail(e, "context streams");
+    }
+    void *p;
+    xs_status s = ctx_alloc(ctx, &p, 256);
+    if (s != XS_OK) {
+        xs_ctx_destroy(ctx);
+        return s;
+    }
+    ctx->s.verification = (unsigned long long *)p;
+    ctx->s.error = (int *)((char *)p + 64);
+    ctx->s.queue = (unsigned int *)((char *)p + 128);
+    Tables &t = ctx->t;
+    t.n_iso = (int)in->n_isotopes;
+    t.n_gp = in->n_gridpoints;
+    t.grid_type = in->grid_type;
+    t.hash_bins = in->hash_bins;
+    t.hash_du = in->hash_bins > 0 ? 1.0 / in->hash_bins : 0.0;
+    pick_mat_thresholds(t.mat_thresh);
+    *out = ctx;
+    return XS_OK;
+}
+
+xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out)
+{
+    if (!out) return fail(XS_ERR_INVALID_ARGUMENT, "xs_ctx_create: out is NULL");
+    *out = nullptr;
+    xs_status s = check_problem(in, sd);
+    if (s != XS_OK) return s;
+    xs_ctx *ctx = nullptr;
+    s = ctx_open(in, device, &ctx);
+    if (s != XS_OK) return s;
+    Tables &t = ctx->t;
+    t.max_nucs = sd->max_num_nucs;
+    const long n_pts = in->n_isotopes * in->n_gridpoints;
+    s = upload(ctx, sd->num_nucs, kMaterials, &t.num_nucs);
+    if (s == XS_OK) s = upload(ctx, sd->mats, (size_t)sd->length_mats, &t.mats);
+    if (s == XS_OK) s = upload(ctx, sd->concs, (size_t)sd->length_concs, &t.concs);
+    if (s == XS_OK) s = upload(ctx, sd->nuclide_grid, (size_t)n_pts, &t.grid);
+    if (s == XS_OK && in->grid_type == XS_UNIONIZED) {
+        t.n_union = sd->length_unionized_energy_array;
+        s = upload(ctx, sd->unionized_energy_array, (size_t)t.n_union, &t.union_e);
+    }
+    if (s == XS_OK && in->grid_type != XS_NUCLIDE)
+        s = upload(ctx, sd->index_grid, (size_t)sd->length_index_grid, &t.index_grid);
+    if (s == XS_OK) s = build_derived_tables(ctx);
+    if (s != XS_OK) {
+        xs_ctx_destroy(ctx);
+        return s;
+    }
+    *out = ctx;
+    return XS_OK;
+}
+
+xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs_ctx **out)
+{
+    (void)in;
+    (void)device;
+    (void)out;
+    return fail(XS_ERR_UNSUPPORTED, "device-side problem setup is not built in this version");
+}
+
+xs_status xs_ctx_download(xs_ctx *ctx, xs_simdata *out)
+{
+    if (!ctx || !out) return fail(XS_ERR_INVALID_ARGUMENT, "xs_ctx_download: NULL argument");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    const Tables &t = ctx->t;
+    xs_simdata r;
+    std::memset(&r, 0, sizeof r);
+    const long n_pts = (long)t.n_iso * t.n_gp;
+    r.length_num_nucs = kMaterials;
+    r.max_num_nucs = t.max_nucs;
+    r.length_mats = r.length_concs = kMaterials * t.max_nucs;
+    r.length_nuclide_grid = (int)n_pts;
+    r.num_nucs = (int *)malloc(sizeof(int) * kMaterials);
+    r.mats = (int *)malloc(sizeof(int) * (size_t)r.length_mats);
+    r.concs = (double *)malloc(sizeof(double) * (size_t)r.length_concs);
+    r.nuclide_grid = (xs_gridpoint *)malloc(sizeof(xs_gridpoint) * (size_t)n_pts);
+    long n_index = 0;
+    if (t.grid_type == XS_UNIONIZED) {
+        r.length_unionized_energy_array = (int)t.n_union;
+        r.unionized_energy_array = (double *)malloc(sizeof(double) * (size_t)t.n_union);
+        n_index = t.n_union * t.n_iso;
+    } else if (t.grid_type == XS_HASH) {
+        n_index = (long)t.hash_bins * t.n_iso;
+    }
+    r.length_index_grid = n_index;
+    if (n_index) r.index_grid = (int *)malloc(sizeof(int) * (size_t)n_index);
+    if (!r.num_nucs || !r.mats || !r.concs || !r.nuclide_grid || (n_index && !r.index_grid) ||
+        (t.grid_type == XS_UNIONIZED && !r.unionized_energy_array)) {
+        xs_simdata_free(&r);
+        return fail(XS_ERR_OUT_OF_MEMORY, "host copies");
+    }
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(r.num_nucs, t.num_nucs, sizeof(int) * kMaterials, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.mats, t.mats, sizeof(int) * (size_t)r.length_mats, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.concs, t.concs, sizeof(double) * (size_t)r.length_concs, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.nuclide_grid, t.grid, sizeof(xs_gridpoint) * (size_t)n_pts, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && r.unionized_energy_array)
+        e = cudaMemcpyAsync(r.unionized_energy_array, t.union_e, sizeof(double) * (size_t)t.n_union, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && n_index)
+        e = cudaMemcpyAsync(r.index_grid, t.index_grid, sizeof(int) * (size_t)n_index, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        xs_simdata_free(&r);
+        return cuda_fail(e, "download");
+    }
+    *out = r;
+    return XS_OK;
+}
+
+xs_status xs_ctx_sync(xs_ctx *ctx, xs_run_result *result)
+{
+    if (!ctx) return fail(XS_ERR_INVALID_ARGUMENT, "xs_ctx_sync: NULL context");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->last_stream ? ctx->last_stream : ctx->stream;
+    xs_status s = read_back(ctx, st, result);
+    if (result) result->kernel_launches = ctx->last_launches;
+    return s;
+}
+
+// Shared by xs_run_event (samples == NULL) and device-resident xs_lookup_samples.
+static xs_status run_once(xs_ctx *ctx, const xs_run_opts &o, const SampleInput &in,
+                          double *macro_out, unsigned char *idx_out, xs_run_result *result)
+{
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : ctx->stream;
+    const long n = o.count;
+    const bool host_macro = macro_out && !is_device_pointer(macro_out);
+    const bool host_idx = idx_out && !is_device_pointer(idx_out);
+    if (o.async && (host_macro || host_idx))
+        return fail(XS_ERR_INVALID_ARGUMENT, "async runs take device (or NULL) output arrays");
+    Outputs out;
+    out.macro = macro_out;
+    out.max_idx = idx_out;
+    if (host_macro || host_idx) {
+        size_t need = (host_macro ? (size_t)n * 40 : 0) + (host_idx ? (size_t)n + 256 : 0);
+        xs_status s = ensure_stage(ctx, need);
+        if (s != XS_OK) return s;
+        char *b = (char *)ctx->s.stage;
+        if (host_macro) {
+            out.macro = (double *)b;
+            b += (size_t)n * 40;
+        }
+        if (host_idx) out.max_idx = (unsigned char *)b;
+    }
+    XS_CUDA(cudaMemsetAsync(ctx->s.verification, 0, 8, st));
+    XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, st));
+    XS_CUDA(cudaEventRecord(ctx->ev0, st));
+    int launches = 0;
+    xs_status s;
+    if (o.kernel == XS_KERNEL_PLAIN)
+        s = launch_plain(ctx, st, o.arith, o.checked, o.first, n, 256, o.tile_lookups, in, out, &launches);
+    else
+        s = launch_batched(ctx, st, o.arith, o.checked, o.first, n, 256, o.energy_buckets, in, out, &launches);
+    if (s != XS_OK) return s;
+    XS_CUDA(cudaEventRecord(ctx->ev1, st));
+    ctx->last_stream = st;
+    ctx->last_launches = launches;
+    if (o.async) {
+        if (result) {
+            result->verification = 0;
+            result->device_ms = 0.f;
+            result->kernel_launches = launches;
+        }
+        return XS_OK;
+    }
+    if (host_macro) XS_CUDA(cudaMemcpyAsync(macro_out, out.macro, (size_t)n * 40, cudaMemcpyDeviceToHost, st));
+    if (host_idx) XS_CUDA(cudaMemcpyAsync(idx_out, out.max_idx, (size_t)n, cudaMemcpyDeviceToHost, st));
+    s = read_back(ctx, st, result);
+    if (result) result->kernel_launches = launches;
+    return s;
+}
+
+xs_status xs_run_event(xs_ctx *ctx, const xs_run_opts *opts, double *macro_xs_out,
+                       unsigned char *max_idx_out, xs_run_result *result)
+{
+    if (!ctx) return fail(XS_ERR_INVALID_ARGUMENT, "xs_run_event: NULL context");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    xs_run_opts o;
+    xs_status s = resolve(ctx, opts, (long)ctx->inputs.lookups, &o);
+    if (s != XS_OK) return s;
+    return run_once(ctx, o, SampleInput{}, macro_xs_out, max_idx_out, result);
+}
+
+// Host-resident samples: chunks alternate between two streams, so the copy
+// of one chunk overlaps the lookups of the other.
+static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *energy,
+                               const int *mat, long n, double *macro_out, unsigned char *idx_out,
+                               xs_run_result *result)
+{
+    const long chunk = o.tile_lookups > 0 && o.kernel == XS_KERNEL_PLAIN ? std::max<long>(1L << 20, o.tile_lookups) : (1L << 21);
+    const size_t per = 8 + 4 + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
+    const size_t need = 2 * ((size_t)chunk * per + 1024);
+    if (ctx->pipe_bytes < need) {
+        if (ctx->pipe_buf) {
+            cudaFree(ctx->pipe_buf);
+            ctx->device_bytes -= ctx->pipe_bytes;
+            ctx->pipe_buf = nullptr;
+            ctx->pipe_bytes = 0;
+            for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+            ctx->graphs.clear();
+        }
+        cudaError_t e = cudaMalloc(&ctx->pipe_buf, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(XS_ERR_OUT_OF_MEMORY, "sample pipeline buffers (%zu bytes)", need);
+        }
+        ctx->pipe_bytes = need;
+        ctx->device_bytes += need;
+    }
+    cudaStream_t main = o.stream ? (cudaStream_t)o.stream : ctx->stream;
+    XS_CUDA(cudaMemsetAsync(ctx->s.verification, 0, 8, main));
+    XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, main));
+    XS_CUDA(cudaEventRecord(ctx->ev0, main));
+    for (int i = 0; i < 2; i++) XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[i], ctx->ev0, 0));
+    int launches = 0;
+    for (long c0 = 0, k = 0; c0 < n; c0 += chunk, k++) {
+        const int w = (int)(k & 1);
+        cudaStream_t st = ctx->pipe_stream[w];
+        const long m = std::min(chunk, n - c0);
+        char *b = (char *)ctx->pipe_buf + (size_t)w * (need / 2);
+        double *dE = (double *)b;
+        int *dM = (int *)(b + (size_t)chunk * 8);
+        double *dMacro = macro_out ? (double *)(b + (size_t)chunk * 12) : nullptr;
+        unsigned char *dIdx = idx_out ? (unsigned char *)(b + (size_t)chunk * (12 + (macro_out ? 40 : 0))) : nullptr;
+        XS_CUDA(cudaMemcpyAsync(dE, energy + c0, (size_t)m * 8, cudaMemcpyHostToDevice, st));
+        XS_CUDA(cudaMemcpyAsync(dM, mat + c0, (size_t)m * 4, cudaMemcpyHostToDevice, st));
+        SampleInput in;
+        in.energy = dE;
+        in.mat = dM;
+        Outputs out;
+        out.macro = dMacro;
+        out.max_idx = dIdx;
+        xs_status s;
+        if (o.kernel == XS_KERNEL_PLAIN)
+            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, 256, o.tile_lookups, in, out, &launches);
+        else
+            s = launch_batched(ctx, st, o.arith, o.checked, 0, m, 256, o.energy_buckets, in, out, &launches);
+        if (s != XS_OK) return s;
+        if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));
+        if (idx_out) XS_CUDA(cudaMemcpyAsync(idx_out + c0, dIdx, (size_t)m, cudaMemcpyDeviceToHost, st));
+        if (o.kernel == XS_KERNEL_BATCHED) {
+            // the batched sort buffers are shared: serialise the two streams
+            XS_CUDA(cudaEventRecord(ctx->pipe_event[w], st));
+            XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[w ^ 1], ctx->pipe_event[w], 0));
+        }
+    }
+    for (int i = 0; i < 2; i++) {
+        XS_CUDA(cudaEventRecord(ctx->pipe_event[i], ctx->pipe_stream[i]));
+        XS_CUDA(cudaStreamWaitEvent(main, ctx->pipe_event[i], 0));
+    }
+    XS_CUDA(cudaEventRecord(ctx->ev1, main));
+    xs_status s = read_back(ctx, main, result);
+    if (result) result->kernel_launches = launches;
+    return s;
+}
+
+xs_status xs_lookup_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
+                            const int *mat, long n, double *macro_xs_out,
+                            unsigned char *max_idx_out, xs_run_result *result)
+{
+    if (!ctx) return fail(XS_ERR_INVALID_ARGUMENT, "xs_lookup_samples: NULL context");
+    if (!energy || !mat || n <= 0) return fail(XS_ERR_INVALID_ARGUMENT, "xs_lookup_samples: need energy, mat and n > 0");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    xs_run_opts o;
+    xs_status s = resolve(ctx, opts, n, &o);
+    if (s != XS_OK) return s;
+    o.first = 0;
+    o.count = n;
+    const bool dev_in = is_device_pointer(energy) && is_device_pointer(mat);
+    if (dev_in) {
+        SampleInput in;
+        in.energy = energy;
+        in.mat = mat;
+        return run_once(ctx, o, in, macro_xs_out, max_idx_out, result);
+    }
+    if (o.async) return fail(XS_ERR_INVALID_ARGUMENT, "async runs take device sample arrays");
+    if (is_device_pointer(energy) || is_device_pointer(mat) ||
+        (macro_xs_out && is_device_pointer(macro_xs_out)) || (max_idx_out && is_device_pointer(max_idx_out)))
+        return fail(XS_ERR_INVALID_ARGUMENT, "host sample arrays need host output arrays");
+    return run_pipelined(ctx, o, energy, mat, n, macro_xs_out, max_idx_out, result);
+}
+
+xs_status xs_sample_event(xs_ctx *ctx, long first, long count, double *energy_out, int *mat_out)
+{
+    if (!ctx || !energy_out || !mat_out || first < 0 || count <= 0)
+        return fail(XS_ERR_INVALID_ARGUMENT, "xs_sample_event: bad argument");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    const bool dev = is_device_pointer(energy_out) && is_device_pointer(mat_out);
+    double *E = energy_out;
+    int *M = mat_out;
+    if (!dev) {
+        xs_status s = ensure_stage(ctx, (size_t)count * 12 + 256);
+        if (s != XS_OK) return s;
+        E = (double *)ctx->s.stage;
+        M = (int *)((char *)ctx->s.stage + (size_t)count * 8);
+    }
+    xs_status s = launch_sample(ctx, ctx->stream, first, count, E, M);
+    if (s != XS_OK) return s;
+    if (!dev) {
+        XS_CUDA(cudaMemcpyAsync(energy_out, E, (size_t)count * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        XS_CUDA(cudaMemcpyAsync(mat_out, M, (size_t)count * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    XS_CUDA(cudaStreamSynchronize(ctx->stream));
+    return XS_OK;
+}
+
+xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *result)
+{
+    if (!ctx) return fail(XS_ERR_INVALID_ARGUMENT, "xs_run_history: NULL context");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    xs_run_opts o;
+    xs_status s = resolve(ctx, opts, (long)ctx->inputs.particles, &o);
+    if (s != XS_OK) return s;
+    if (ctx->inputs.lookups < 1) return fail(XS_ERR_INVALID_ARGUMENT, "lookups per particle < 1");
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : ctx->stream;
+    XS_CUDA(cudaMemsetAsync(ctx->s.verification, 0, 8, st));
+    XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, st));
+    XS_CUDA(cudaEventRecord(ctx->ev0, st));
+    int launches = 0;
+    s = launch_history(ctx, st, o.arith, o.first, o.count, &launches);
+    if (s != XS_OK) return s;
+    XS_CUDA(cudaEventRecord(ctx->ev1, st));
+    s = read_back(ctx, st, result);
+    if (result) result->kernel_launches = launches;
+    return s;
+}
+
+xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gbar,
+                         double *d_concs, double *d_xs, double *d_energy, xs_run_result *result)
+{
+    (void)ctx; (void)opts; (void)gbar; (void)d_concs; (void)d_xs; (void)d_energy; (void)result;
+    return fail(XS_ERR_UNSUPPORTED, "adjoint is not built in this version");
+}
+
+xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best)
+{
+    (void)ctx; (void)cache_path; (void)best;
+    return fail(XS_ERR_UNSUPPORTED, "autotuner is not built in this version");
+}
+
+xs_status xs_run_event_based_simulation(xs_inputs in, xs_simdata sd, int mype,
+                                        unsigned long long *verification)
+{
+    (void)mype;
+    if (!verification) return fail(XS_ERR_INVALID_ARGUMENT, "verification is NULL");
+    xs_ctx *ctx = nullptr;
+    xs_status s = xs_ctx_create(&in, &sd, 0, &ctx);
+    if (s != XS_OK) return s;
+    xs_run_result r;
+    s = xs_run_event(ctx, nullptr, nullptr, nullptr, &r);
+    if (s == XS_OK) *verification = r.verification;
+    xs_ctx_destroy(ctx);
+    return s;
+}
+
+}  // extern "C"

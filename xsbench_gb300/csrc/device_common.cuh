@@ -1,0 +1,307 @@
+// device_common.cuh -- per-lookup device code shared by the lookup kernels.
+//
+// One thread computes one macroscopic lookup (the body of the reference's
+// event loop, openmp-threading/Simulation.c:62-110): sample, locate the energy
+// in the acceleration structure, interpolate every nuclide of the material and
+// accumulate in list order.  The kernels around it arrange for the 32 lanes of
+// a warp to share the material, so the nuclide loop does not diverge.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xsgb_internal.h"
+
+namespace xsgb {
+
+// ------------------------------------------------------------------- LCG ---
+// Simulation.c:462-499: x <- (a x + 1) mod 2^63, value x / 2^63.
+constexpr unsigned long long kLcgMul = 2806196910506780709ULL;
+constexpr unsigned long long kLcgMask = (1ULL << 63) - 1ULL;
+
+__host__ __device__ __forceinline__ double lcg_next(unsigned long long &s)
+{
+    s = (kLcgMul * s + 1ULL) & kLcgMask;
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(__ull2double_rn(s), 0x1p-63);  // exact scaling by 2^-63
+#else
+    return (double)s * 0x1p-63;
+#endif
+}
+
+__host__ __device__ __forceinline__ unsigned long long lcg_skip(unsigned long long seed,
+                                                                unsigned long long n)
+{
+    unsigned long long mul = kLcgMul, inc = 1ULL, am = 1ULL, ai = 0ULL;
+    n &= kLcgMask;
+    while (n) {
+        if (n & 1ULL) {
+            am *= mul;
+            ai = ai * mul + inc;
+        }
+        inc *= (mul + 1ULL);
+        mul *= mul;
+        n >>= 1;
+    }
+    return (am * seed + ai) & kLcgMask;
+}
+
+// Simulation.c:426-460: the first material whose running sum exceeds the roll;
+// the running sums are precomputed on the host in the reference's order.
+__device__ __forceinline__ int pick_mat(const Tables &t, unsigned long long &s)
+{
+    double roll = lcg_next(s);
+#pragma unroll
+    for (int m = 1; m < kMaterials; m++)
+        if (roll < t.mat_thresh[m]) return m;
+    return 0;
+}
+
+// ----------------------------------------------------------- order keys ---
+// Signed 64-bit keys that order like the doubles they come from (-0 == +0).
+__host__ __device__ __forceinline__ long long order_key(double x)
+{
+#ifdef __CUDA_ARCH__
+    long long b = __double_as_longlong(x);
+#else
+    long long b;
+    __builtin_memcpy(&b, &x, 8);
+#endif
+    if (b < 0) b = (b == (long long)0x8000000000000000ULL) ? 0 : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+    return b;
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T *p)
+{
+    return __ldg(p);
+}
+
+// Error reporting from checked kernels: first error wins.
+__device__ __forceinline__ void report(int *err, int code, long a, long b)
+{
+    if (atomicCAS(err, 0, code) == 0) {
+        err[1] = (int)a;
+        err[2] = (int)b;
+    }
+}
+
+// ------------------------------------------------------- union-grid row ---
+// grid_search (Simulation.c:380-400) returns clamp(#{A <= E} - 1, 0, n - 2) on
+// a sorted array; the accelerator narrows #{A <= E} to one bin of [0,1).
+__device__ __forceinline__ long union_row(const Tables &t, double E)
+{
+    const long n = t.n_union;
+    long c;
+    if (E >= 0.0 && E < 1.0) {
+        const int b = (int)(E * (double)(1 << t.union_bin_log2));
+        long lo = ldg(&t.union_bins[b]), hi = ldg(&t.union_bins[b + 1]);
+        const long long q = order_key(E);
+        while (lo < hi) {
+            long mid = (lo + hi) >> 1;
+            if (ldg(&t.union_keys[mid]) <= q) lo = mid + 1; else hi = mid;
+        }
+        c = lo;
+    } else {
+        // outside [0,1) or NaN: the reference loop with its own comparison
+        long lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            long mid = lo + (hi - lo) / 2;
+            if (ldg(&t.union_e[mid]) > E) hi = mid; else lo = mid;
+        }
+        return lo;
+    }
+    c -= 1;
+    if (c < 0) c = 0;
+    if (c > n - 2) c = n - 2;
+    return c;
+}
+
+// ------------------------------------------------ per-nuclide intervals ---
+// Each returns the index k of the lower gridpoint, already clamped to
+// [0, n_gp-2] the way calculate_micro_xs does it (Simulation.c:259-262,
+// :268-271, :298-301).
+
+// UNIONIZED (Simulation.c:264-272)
+template <bool CHECKED>
+__device__ __forceinline__ long interval_unionized(const Tables &t, long row, int nuc, int *err)
+{
+    long k = ldg(&t.index_grid[row * t.n_iso + nuc]);
+    if (CHECKED && (k < 0 || k > t.n_gp - 1)) {
+        report(err, XS_ERR_DATA, row, nuc);
+        k = 0;
+    }
+    return (k == t.n_gp - 1) ? k - 1 : k;
+}
+
+// NUCLIDE (Simulation.c:252-263): clamp(#{E_j <= E} - 1, 0, n_gp-2), found in a
+// coarse key array (every 16th energy) and then inside one 128-byte line.
+__device__ __forceinline__ long interval_nuclide(const Tables &t, int nuc, long long q)
+{
+    const long long *ck = t.coarse + (long)nuc * t.n_coarse;
+    long lo = 0, hi = t.n_coarse;
+    while (lo < hi) {
+        long mid = (lo + hi) >> 1;
+        if (ldg(&ck[mid]) <= q) lo = mid + 1; else hi = mid;
+    }
+    long ub;
+    if (lo == 0) {
+        ub = 0;
+    } else {
+        const long long *k = t.ekeys + (long)nuc * t.n_gp;
+        long a = (lo - 1) * kCoarseStride + 1;
+        long b = lo * kCoarseStride;
+        if (b > t.n_gp) b = t.n_gp;
+        while (a < b) {
+            long mid = (a + b) >> 1;
+            if (ldg(&k[mid]) <= q) a = mid + 1; else b = mid;
+        }
+        ub = a;
+    }
+    long kk = ub - 1;
+    if (kk < 0) kk = 0;
+    if (kk > t.n_gp - 2) kk = t.n_gp - 2;
+    return kk;
+}
+
+// HASH (Simulation.c:273-302), including its edge rules: E <= e_low gives
+// gridpoint 0, E >= e_high gives the last interval.
+template <bool CHECKED>
+__device__ __forceinline__ long interval_hash(const Tables &t, long bin, int nuc, long long q,
+                                              int *err)
+{
+    const long n_gp = t.n_gp;
+    long u_low = ldg(&t.index_grid[bin * t.n_iso + nuc]);
+    long u_high = (bin == t.hash_bins - 1) ? n_gp - 1
+                                           : (long)ldg(&t.index_grid[(bin + 1) * t.n_iso + nuc]) + 1;
+    if (CHECKED && (u_low < 0 || u_low > n_gp - 1 || u_high < 0 || u_high > n_gp - 1)) {
+        report(err, XS_ERR_DATA, bin, nuc);
+        u_low = 0;
+        u_high = n_gp - 1;
+    }
+    const long long *k = t.ekeys + (long)nuc * n_gp;
+    long lower;
+    if (q <= ldg(&k[u_low])) {
+        lower = 0;
+    } else if (q >= ldg(&k[u_high])) {
+        lower = n_gp - 1;
+    } else {
+        long lo = u_low, hi = u_high;
+        while (hi - lo > 1) {
+            long mid = lo + (hi - lo) / 2;
+            if (ldg(&k[mid]) > q) hi = mid; else lo = mid;
+        }
+        lower = lo;
+    }
+    return (lower == n_gp - 1) ? lower - 1 : lower;
+}
+
+// --------------------------------------------------------- interpolation ---
+// FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record.
+__device__ __forceinline__ void accumulate_fast(const Tables &t, int nuc, long k, double E,
+                                                double conc, double macro[5])
+{
+    const double2 *r = t.records + ((long)nuc * (t.n_gp - 1) + k) * 6;
+    const double2 r0 = ldg(r + 0), r1 = ldg(r + 1), r2 = ldg(r + 2);
+    const double2 r3 = ldg(r + 3), r4 = ldg(r + 4), r5 = ldg(r + 5);
+    const double d = r0.x - E;
+    macro[0] = fma(fma(-d, r3.x, r0.y), conc, macro[0]);
+    macro[1] = fma(fma(-d, r3.y, r1.x), conc, macro[1]);
+    macro[2] = fma(fma(-d, r4.x, r1.y), conc, macro[2]);
+    macro[3] = fma(fma(-d, r4.y, r2.x), conc, macro[3]);
+    macro[4] = fma(fma(-d, r5.x, r2.y), conc, macro[4]);
+    (void)r5;
+}
+
+// EXACT: the reference's operations in its order (Simulation.c:304-322,
+// :372-373), no contraction, IEEE division.
+__device__ __forceinline__ void accumulate_exact(const Tables &t, int nuc, long k, double E,
+                                                 double conc, double macro[5])
+{
+    const double2 *g = reinterpret_cast<const double2 *>(t.grid + (long)nuc * t.n_gp + k);
+    const double2 l0 = ldg(g + 0), l1 = ldg(g + 1), l2 = ldg(g + 2);
+    const double2 h0 = ldg(g + 3), h1 = ldg(g + 4), h2 = ldg(g + 5);
+    const double f = __ddiv_rn(__dsub_rn(h0.x, E), __dsub_rn(h0.x, l0.x));
+    const double lo[5] = {l0.y, l1.x, l1.y, l2.x, l2.y};
+    const double hi[5] = {h0.y, h1.x, h1.y, h2.x, h2.y};
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        double xs = __dsub_rn(hi[c], __dmul_rn(f, __dsub_rn(hi[c], lo[c])));
+        macro[c] = __dadd_rn(macro[c], __dmul_rn(xs, conc));
+    }
+}
+
+// Simulation.c:100-110
+__device__ __forceinline__ int argmax5(const double m[5])
+{
+    double best = -1.0;
+    int arg = 0;
+#pragma unroll
+    for (int c = 0; c < 5; c++)
+        if (m[c] > best) {
+            best = m[c];
+            arg = c;
+        }
+    return arg;
+}
+
+// ------------------------------------------------------------ one lookup ---
+// calculate_macro_xs (Simulation.c:326-375) for one (E, mat).
+template <int GRID, int ARITH, bool CHECKED>
+__device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, double macro[5],
+                                         int *err)
+{
+#pragma unroll
+    for (int c = 0; c < 5; c++) macro[c] = 0.0;
+    const int n = ldg(&t.num_nucs[mat]);
+    const int *mrow = t.mats + mat * t.max_nucs;
+    const double *crow = t.concs + mat * t.max_nucs;
+    long row = 0;
+    long long q = 0;
+    const bool keyed = !(E != E);   // NaN energies use the double-compare path
+    if (GRID == XS_UNIONIZED) {
+        row = union_row(t, E);
+    } else if (GRID == XS_HASH) {
+        row = (long)(E / t.hash_du);  // Simulation.c:350-351
+        if (row < 0 || row > t.hash_bins - 1) {
+            // the reference reads outside its table here; clamp instead
+            if (CHECKED) report(err, XS_ERR_DATA, row, -1);
+            row = row < 0 ? 0 : t.hash_bins - 1;
+        }
+        q = order_key(E);
+    } else {
+        q = order_key(E);
+    }
+#pragma unroll 2
+    for (int j = 0; j < n; j++) {
+        const int nuc = ldg(&mrow[j]);
+        const double conc = ldg(&crow[j]);
+        long k;
+        if (GRID == XS_UNIONIZED) {
+            k = interval_unionized<CHECKED>(t, row, nuc, err);
+        } else if (GRID == XS_NUCLIDE) {
+            if (keyed) {
+                k = interval_nuclide(t, nuc, q);
+            } else {
+                k = t.n_gp - 2;  // NaN compares false: the search ends at the top
+            }
+        } else {
+            if (keyed) {
+                k = interval_hash<CHECKED>(t, row, nuc, q, err);
+            } else {
+                long u_high = (row == t.hash_bins - 1)
+                                  ? t.n_gp - 1
+                                  : (long)ldg(&t.index_grid[(row + 1) * t.n_iso + nuc]) + 1;
+                k = u_high - 1;
+                if (k < 0) k = 0;
+                if (k > t.n_gp - 2) k = t.n_gp - 2;
+            }
+        }
+        if (ARITH == XS_ARITH_EXACT)
+            accumulate_exact(t, nuc, k, E, conc, macro);
+        else
+            accumulate_fast(t, nuc, k, E, conc, macro);
+    }
+}
+
+}  // namespace xsgb

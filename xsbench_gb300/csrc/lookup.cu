@@ -1,0 +1,327 @@
+// lookup.cu -- orchestration of the lookup kernels and the on-device
+// counting sort of the batched form.
+//
+// The batched form replaces the reference's optimisation 6
+// (cuda/Simulation.cu:1024-1099: sampling_kernel, 12 thrust::count, a
+// thrust::sort_by_key by material and 12 by energy, 12 launches of
+// xs_lookup_kernel_optimization_4, thrust::reduce) by four kernels captured in
+// one CUDA graph: histogram of (material, energy bucket) keys, one-block scan,
+// scatter, and one persistent lookup kernel whose block sums are added into the
+// verification counter.
+#include <cstdio>
+#include <cstring>
+
+#include "lookup_kernels.cuh"
+
+namespace xsgb {
+
+// ------------------------------------------------------------ sort pass ---
+constexpr int kSortLpt = 8;  // lookups per thread in the sampling passes
+
+__device__ __forceinline__ int energy_bucket(double E, int nb_log2)
+{
+    const int nb = 1 << nb_log2;
+    if (E >= 0.0 && E < 1.0) return (int)(E * (double)nb);
+    return (E >= 1.0) ? nb - 1 : 0;  // NaN and negatives go to bucket 0
+}
+
+template <bool SAMPLES, bool SCATTER>
+__global__ void __launch_bounds__(kBlock) k_sort_pass(Tables t, long first, long count,
+                                                      int nb_log2, const double *in_E,
+                                                      const int *in_mat, int *offs, double *sE,
+                                                      int *sid, int *err)
+{
+    const long g = (long)blockIdx.x * kBlock + threadIdx.x;
+    if (SAMPLES) {
+        // coalesced stride over the caller's arrays
+        const long stride = (long)gridDim.x * kBlock;
+        for (long i = g; i < count; i += stride) {
+            unsigned long long seed = 0;
+            double E;
+            int m;
+            if (!sample_at<true>(t, in_E, in_mat, i, seed, E, m, err)) continue;
+            const int key = (m << nb_log2) + energy_bucket(E, nb_log2);
+            if (SCATTER) {
+                const int pos = atomicAdd(&offs[key], 1);
+                sE[pos] = E;
+                sid[pos] = (int)i;
+            } else {
+                atomicAdd(&offs[key], 1);
+            }
+        }
+    } else {
+        const long i0 = g * kSortLpt;
+        if (i0 >= count) return;
+        unsigned long long seed = lcg_skip(kStartingSeed, 2ULL * (unsigned long long)(first + i0));
+        for (int q = 0; q < kSortLpt && i0 + q < count; q++) {
+            double E;
+            int m;
+            sample_at<false>(t, nullptr, nullptr, 0, seed, E, m, err);
+            const int key = (m << nb_log2) + energy_bucket(E, nb_log2);
+            if (SCATTER) {
+                const int pos = atomicAdd(&offs[key], 1);
+                sE[pos] = E;
+                sid[pos] = (int)(i0 + q);
+            } else {
+                atomicAdd(&offs[key], 1);
+            }
+        }
+    }
+}
+
+// One block turns the (material, bucket) histogram into scatter offsets.
+// Each material's run starts on a multiple of 32 entries, so every 32-entry
+// chunk of the sorted list holds one material only.
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) k_sort_scan(int *offs, int nb_log2, int *seg,
+                                                            int *cnt)
+{
+    __shared__ int warp_tot[32];
+    __shared__ int base;
+    const int nb = 1 << nb_log2;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int per = (nb + kScanThreads - 1) / kScanThreads;
+    if (tid == 0) base = 0;
+    __syncthreads();
+    for (int m = 0; m < kMaterials; m++) {
+        int *h = offs + (m << nb_log2);
+        const int b0 = tid * per, b1 = min(nb, b0 + per);
+        int s = 0;
+        for (int b = b0; b < b1; b++) s += h[b];
+        // inclusive warp scan
+        int v = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) warp_tot[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            int w = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_tot[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        const int total = warp_tot[31];
+        int run = base + (v - s) + (warp ? warp_tot[warp - 1] : 0);
+        for (int b = b0; b < b1; b++) {
+            int c = h[b];
+            h[b] = run;
+            run += c;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            cnt[m] = total;
+            seg[m] = base;
+            base += (total + 31) & ~31;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) seg[kMaterials] = base;
+}
+
+// Simulation.c:735-750: the samples alone, one thread per 8 consecutive lookups
+__global__ void __launch_bounds__(kBlock) k_sample(Tables t, long first, long count, double *E,
+                                                   int *mat)
+{
+    const long i0 = ((long)blockIdx.x * kBlock + threadIdx.x) * kSortLpt;
+    if (i0 >= count) return;
+    unsigned long long seed = lcg_skip(kStartingSeed, 2ULL * (unsigned long long)(first + i0));
+    for (int q = 0; q < kSortLpt && i0 + q < count; q++) {
+        E[i0 + q] = lcg_next(seed);
+        mat[i0 + q] = pick_mat(t, seed);
+    }
+}
+
+xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat)
+{
+    const unsigned blocks = (unsigned)((count + (long)kBlock * kSortLpt - 1) / ((long)kBlock * kSortLpt));
+    k_sample<<<blocks, kBlock, 0, st>>>(ctx->t, first, count, E, mat);
+    XS_CUDA(cudaGetLastError());
+    return XS_OK;
+}
+
+size_t batched_scratch_bytes(long count, int buckets)
+{
+    const size_t padded = (size_t)count + kMaterials * 32;
+    size_t b = (size_t)kMaterials * buckets * 4;   // offsets
+    b = (b + 255) & ~(size_t)255;
+    b += 256;                                       // seg[13] + cnt[12]
+    b += padded * 8;                                // sorted energies
+    b = (b + 255) & ~(size_t)255;
+    b += padded * 4;                                // original ids
+    return b + 256;
+}
+
+static int ilog2(int x)
+{
+    int l = 0;
+    while ((1 << l) < x) l++;
+    return l;
+}
+
+typedef cudaError_t (*PlainFn)(const Tables &, cudaStream_t, int, int, bool, long, long, int,
+                               const double *, const int *, double *, unsigned char *,
+                               unsigned long long *, int *);
+typedef cudaError_t (*BatchedFn)(const Tables &, cudaStream_t, int, int, int, const int *,
+                                 const int *, const double *, const int *, unsigned int *,
+                                 double *, unsigned char *, unsigned long long *, int *);
+typedef cudaError_t (*HistoryFn)(const Tables &, cudaStream_t, int, long, long, int,
+                                 unsigned long long *, int *);
+
+static PlainFn plain_fn(int g)
+{
+    return g == XS_UNIONIZED ? unionized_plain : g == XS_NUCLIDE ? nuclide_plain : hash_plain;
+}
+static BatchedFn batched_fn(int g)
+{
+    return g == XS_UNIONIZED ? unionized_batched : g == XS_NUCLIDE ? nuclide_batched : hash_batched;
+}
+static HistoryFn history_fn(int g)
+{
+    return g == XS_UNIONIZED ? unionized_history : g == XS_NUCLIDE ? nuclide_history : hash_history;
+}
+
+xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                       long count, int block, int tile, const SampleInput &in,
+                       const Outputs &out, int *launches)
+{
+    (void)block;
+    if (tile < kBlock || tile % kBlock) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d must be a multiple of %d", tile, kBlock);
+    if (tile > 8192) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d above 8192", tile);
+    XS_CUDA(plain_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, in.energy != nullptr, first,
+                                       count, tile, in.energy, in.mat, out.macro, out.max_idx,
+                                       ctx->s.verification, ctx->s.error));
+    if (launches) *launches += 1;
+    return XS_OK;
+}
+
+// Enqueues the batched pipeline on `st` (used directly or under capture).
+static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                                 long count, int nb_log2, const SampleInput &in,
+                                 const Outputs &out, int *launches)
+{
+    const int nb = 1 << nb_log2;
+    char *b = (char *)ctx->s.sort_buf;
+    int *offs = (int *)b;
+    size_t off = ((size_t)kMaterials * nb * 4 + 255) & ~(size_t)255;
+    int *seg = (int *)(b + off);
+    int *cnt = seg + 16;
+    off += 256;
+    double *sE = (double *)(b + off);
+    off += ((size_t)count + kMaterials * 32) * 8;
+    off = (off + 255) & ~(size_t)255;
+    int *sid = (int *)(b + off);
+
+    XS_CUDA(cudaMemsetAsync(offs, 0, (size_t)kMaterials * nb * 4, st));
+    XS_CUDA(cudaMemsetAsync(ctx->s.queue, 0, sizeof(unsigned int), st));
+    const bool samples = in.energy != nullptr;
+    unsigned blocks;
+    if (samples) {
+        long want = (count + kBlock - 1) / kBlock;
+        long cap = (long)ctx->sm_count * 8;
+        blocks = (unsigned)(want < cap ? want : cap);
+        if (blocks == 0) blocks = 1;
+        k_sort_pass<true, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+    } else {
+        blocks = (unsigned)((count + (long)kBlock * kSortLpt - 1) / ((long)kBlock * kSortLpt));
+        k_sort_pass<false, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+    }
+    XS_CUDA(cudaGetLastError());
+    k_sort_scan<<<1, kScanThreads, 0, st>>>(offs, nb_log2, seg, cnt);
+    XS_CUDA(cudaGetLastError());
+    if (samples)
+        k_sort_pass<true, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+    else
+        k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+    XS_CUDA(cudaGetLastError());
+    const int lookup_blocks = ctx->sm_count * ctx->batched_blocks_per_sm;
+    XS_CUDA(batched_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, lookup_blocks, seg, cnt, sE,
+                                         sid, ctx->s.queue, out.macro, out.max_idx,
+                                         ctx->s.verification, ctx->s.error));
+    if (launches) *launches += 4;
+    return XS_OK;
+}
+
+xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                         long count, int block, int buckets, const SampleInput &in,
+                         const Outputs &out, int *launches)
+{
+    (void)block;
+    if (buckets < 1 || (buckets & (buckets - 1)) || buckets > 65536)
+        return fail(XS_ERR_INVALID_ARGUMENT, "energy_buckets %d must be a power of two <= 65536", buckets);
+    if (count > 0x7FFFFFFFL - kMaterials * 32)
+        return fail(XS_ERR_INVALID_ARGUMENT, "batched runs take at most 2^31 - 385 lookups");
+    const int nb_log2 = ilog2(buckets);
+    const size_t need = batched_scratch_bytes(count, buckets);
+    if (ctx->s.sort_bytes < need) {
+        for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+        ctx->graphs.clear();
+        if (ctx->s.sort_buf) {
+            cudaFree(ctx->s.sort_buf);
+            ctx->device_bytes -= ctx->s.sort_bytes;
+            ctx->s.sort_buf = nullptr;
+            ctx->s.sort_bytes = 0;
+        }
+        cudaError_t e = cudaMalloc(&ctx->s.sort_buf, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(XS_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes for the batched sort failed", need);
+        }
+        ctx->s.sort_bytes = need;
+        ctx->device_bytes += need;
+    }
+    char key[256];
+    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d", arith, checked, first, count,
+             nb_log2, (const void *)in.energy, (const void *)in.mat, (void *)out.macro,
+             (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+        cudaStream_t cap;
+        XS_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return cuda_fail(e, "cudaStreamBeginCapture");
+        }
+        int n = 0;
+        xs_status s = enqueue_batched(ctx, cap, arith, checked, first, count, nb_log2, in, out, &n);
+        e = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (s != XS_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        BatchedGraph bg;
+        e = cudaGraphInstantiate(&bg.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        bg.launches = n;
+        if (ctx->graphs.size() > 64) {
+            for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
+            ctx->graphs.clear();
+        }
+        it = ctx->graphs.emplace(key, bg).first;
+    }
+    XS_CUDA(cudaGraphLaunch(it->second.exec, st));
+    if (launches) *launches += it->second.launches;
+    return XS_OK;
+}
+
+xs_status launch_history(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                         int *launches)
+{
+    XS_CUDA(history_fn(ctx->t.grid_type)(ctx->t, st, arith, first, count, ctx->inputs.lookups,
+                                         ctx->s.verification, ctx->s.error));
+    if (launches) *launches += 1;
+    return XS_OK;
+}
+
+}  // namespace xsgb

@@ -1,0 +1,156 @@
+// tables.cu -- device-side tables derived from the reference arrays at
+// context creation, and the validation pass that lets the lookup kernels
+// index without bounds checks.
+//
+//   records     per nuclide interval k: E_hi, the five xs at k+1, the five
+//               slopes (xs_{k+1}-xs_k)/(E_{k+1}-E_k) and E_lo (96 bytes)
+//   ekeys       order keys of every gridpoint energy (HASH / NUCLIDE searches)
+//   coarse      every 16th key of each nuclide (NUCLIDE search, first level)
+//   union_keys  order keys of the unionized energies
+//   union_bins  for b = 0..2^L: #{union energies < b / 2^L}
+#include "device_common.cuh"
+
+namespace xsgb {
+
+__global__ void k_records(const xs_gridpoint *grid, long n_iso, long n_gp, double2 *rec)
+{
+    const long n_int = n_gp - 1;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n_iso * n_int;
+         i += (long)gridDim.x * blockDim.x) {
+        const long nuc = i / n_int, k = i - nuc * n_int;
+        const xs_gridpoint lo = grid[nuc * n_gp + k];
+        const xs_gridpoint hi = grid[nuc * n_gp + k + 1];
+        const double dE = hi.energy - lo.energy;
+        double2 *r = rec + i * 6;
+        r[0] = make_double2(hi.energy, hi.total_xs);
+        r[1] = make_double2(hi.elastic_xs, hi.absorbtion_xs);
+        r[2] = make_double2(hi.fission_xs, hi.nu_fission_xs);
+        r[3] = make_double2((hi.total_xs - lo.total_xs) / dE, (hi.elastic_xs - lo.elastic_xs) / dE);
+        r[4] = make_double2((hi.absorbtion_xs - lo.absorbtion_xs) / dE,
+                            (hi.fission_xs - lo.fission_xs) / dE);
+        r[5] = make_double2((hi.nu_fission_xs - lo.nu_fission_xs) / dE, lo.energy);
+    }
+}
+
+__global__ void k_grid_keys(const xs_gridpoint *grid, long n, long long *keys)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x)
+        keys[i] = order_key(grid[i].energy);
+}
+
+__global__ void k_coarse(const long long *ekeys, long n_iso, long n_gp, int n_coarse,
+                         long long *coarse)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n_iso * n_coarse;
+         i += (long)gridDim.x * blockDim.x) {
+        const long nuc = i / n_coarse, c = i - nuc * n_coarse;
+        coarse[i] = ekeys[nuc * n_gp + c * kCoarseStride];
+    }
+}
+
+__global__ void k_double_keys(const double *v, long n, long long *keys)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x)
+        keys[i] = order_key(v[i]);
+}
+
+__global__ void k_union_bins(const long long *keys, long n, int log2b, int *bins)
+{
+    const long nb = 1L << log2b;
+    for (long b = (long)blockIdx.x * blockDim.x + threadIdx.x; b <= nb;
+         b += (long)gridDim.x * blockDim.x) {
+        const long long q = order_key((double)b / (double)nb);
+        long lo = 0, hi = n;  // first index with key >= q
+        while (lo < hi) {
+            long mid = (lo + hi) >> 1;
+            if (keys[mid] < q) lo = mid + 1; else hi = mid;
+        }
+        bins[b] = (int)lo;
+    }
+}
+
+// Range checks of caller-supplied tables; err[0] = 1 on the first failure.
+__global__ void k_check_index(const int *idx, long n, int lo, int hi, int *err)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long)gridDim.x * blockDim.x) {
+        const int v = idx[i];
+        if (v < lo || v > hi) report(err, XS_ERR_DATA, i, v);
+    }
+}
+
+static unsigned grid_for(long n, int sm)
+{
+    long b = (n + 255) / 256;
+    long cap = (long)sm * 32;
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+xs_status build_derived_tables(xs_ctx *ctx)
+{
+    Tables &t = ctx->t;
+    cudaStream_t st = ctx->stream;
+    const int sm = ctx->sm_count;
+    const long n_points = (long)t.n_iso * t.n_gp;
+
+    // validation of the integer tables the kernels index with
+    XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 4 * sizeof(int), st));
+    if (t.grid_type == XS_UNIONIZED)
+        k_check_index<<<grid_for((long)t.n_union * t.n_iso, sm), 256, 0, st>>>(
+            t.index_grid, (long)t.n_union * t.n_iso, 0, (int)(t.n_gp - 1), ctx->s.error);
+    if (t.grid_type == XS_HASH)
+        k_check_index<<<grid_for((long)t.hash_bins * t.n_iso, sm), 256, 0, st>>>(
+            t.index_grid, (long)t.hash_bins * t.n_iso, 0, (int)(t.n_gp - 2), ctx->s.error);
+    XS_CUDA(cudaGetLastError());
+
+    // interval records for the fast arithmetic
+    void *p = nullptr;
+    xs_status s = ctx_alloc(ctx, &p, (size_t)t.n_iso * (t.n_gp - 1) * 96);
+    if (s != XS_OK) return s;
+    t.records = (const double2 *)p;
+    k_records<<<grid_for(t.n_iso * (t.n_gp - 1), sm), 256, 0, st>>>(t.grid, t.n_iso, t.n_gp, (double2 *)p);
+    XS_CUDA(cudaGetLastError());
+
+    if (t.grid_type != XS_UNIONIZED) {
+        s = ctx_alloc(ctx, &p, (size_t)n_points * 8);
+        if (s != XS_OK) return s;
+        t.ekeys = (const long long *)p;
+        k_grid_keys<<<grid_for(n_points, sm), 256, 0, st>>>(t.grid, n_points, (long long *)p);
+        XS_CUDA(cudaGetLastError());
+    }
+    if (t.grid_type == XS_NUCLIDE) {
+        t.n_coarse = (int)((t.n_gp + kCoarseStride - 1) / kCoarseStride);
+        s = ctx_alloc(ctx, &p, (size_t)t.n_iso * t.n_coarse * 8);
+        if (s != XS_OK) return s;
+        t.coarse = (const long long *)p;
+        k_coarse<<<grid_for((long)t.n_iso * t.n_coarse, sm), 256, 0, st>>>(t.ekeys, t.n_iso, t.n_gp, t.n_coarse, (long long *)p);
+        XS_CUDA(cudaGetLastError());
+    }
+    if (t.grid_type == XS_UNIONIZED) {
+        s = ctx_alloc(ctx, &p, (size_t)t.n_union * 8);
+        if (s != XS_OK) return s;
+        t.union_keys = (const long long *)p;
+        k_double_keys<<<grid_for(t.n_union, sm), 256, 0, st>>>(t.union_e, t.n_union, (long long *)p);
+        XS_CUDA(cudaGetLastError());
+        // about one union energy per bin, at least 2^10 and at most 2^26 bins
+        int lb = 10;
+        while (lb < 26 && (1L << lb) < t.n_union) lb++;
+        t.union_bin_log2 = lb;
+        s = ctx_alloc(ctx, &p, ((size_t)(1L << lb) + 1) * 4);
+        if (s != XS_OK) return s;
+        t.union_bins = (const int *)p;
+        k_union_bins<<<grid_for((1L << lb) + 1, sm), 256, 0, st>>>(t.union_keys, t.n_union, lb, (int *)p);
+        XS_CUDA(cudaGetLastError());
+    }
+    int herr[4] = {0, 0, 0, 0};
+    XS_CUDA(cudaMemcpyAsync(herr, ctx->s.error, sizeof herr, cudaMemcpyDeviceToHost, st));
+    XS_CUDA(cudaStreamSynchronize(st));
+    if (herr[0])
+        return fail(XS_ERR_DATA, "table entry out of range (position %d, value %d)", herr[1], herr[2]);
+    return XS_OK;
+}
+
+}  // namespace xsgb

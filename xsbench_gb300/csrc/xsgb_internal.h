@@ -1,0 +1,133 @@
+// xsgb_internal.h -- shared declarations of the GB300 lookup library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/xsgb.h"
+
+namespace xsgb {
+
+constexpr int kMaterials = 12;
+constexpr int kRecordDoubles = 12;      // fast-mode interval record, 96 bytes
+constexpr int kCoarseStride = 16;       // NUCLIDE grid: one coarse key per 16 energies
+constexpr unsigned long long kStartingSeed = 1070ULL;  // XSbench_header.h:51
+
+// Record layout of interval k of nuclide n (fast arithmetic):
+//   [0] E_hi  [1..5] xs_hi[5]  [6..10] slope[5] = (hi-lo)/(E_hi-E_lo)  [11] E_lo
+// One record is 96 bytes = three 32-byte sectors, 16-byte aligned.
+
+// Read-only device view of one problem, passed by value to the kernels.
+struct Tables {
+    int n_iso;
+    int grid_type;
+    long n_gp;
+    int hash_bins;
+    int max_nucs;
+    double hash_du;                  // 1.0 / hash_bins, as the reference computes it
+    long n_union;
+    int union_bin_log2;              // union accelerator: 2^b bins over [0,1)
+    int n_coarse;                    // coarse keys per nuclide (NUCLIDE grid)
+    const int *num_nucs;             // [12]
+    const int *mats;                 // [12 * max_nucs]
+    const double *concs;             // [12 * max_nucs]
+    const xs_gridpoint *grid;        // [n_iso * n_gp]  reference AoS
+    const double2 *records;          // [n_iso * (n_gp-1) * 6] fast records
+    const long long *ekeys;          // [n_iso * n_gp]  order keys of grid energies
+    const long long *coarse;         // [n_iso * n_coarse]
+    const double *union_e;           // [n_union]
+    const long long *union_keys;     // [n_union]
+    const int *union_bins;           // [2^b + 1]
+    const int *index_grid;           // UEG: [n_union * n_iso]  HASH: [hash_bins * n_iso]
+    double mat_thresh[kMaterials];   // pick_mat running sums, Simulation.c:450-457
+};
+
+// Per-run scratch in device memory (owned by the context).
+struct Scratch {
+    unsigned long long *verification = nullptr;  // 1 counter
+    int *error = nullptr;                        // 1 flag + 3 detail words
+    unsigned int *queue = nullptr;               // work-queue counter
+    void *sort_buf = nullptr;                    // batched sort buffers
+    size_t sort_bytes = 0;
+    void *stage = nullptr;                       // staging for host outputs
+    size_t stage_bytes = 0;
+};
+
+struct BatchedGraph {
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+};
+
+}  // namespace xsgb
+
+struct xs_ctx {
+    int device = 0;
+    xs_inputs inputs{};
+    std::string hm;
+    xsgb::Tables t{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void *> allocations;
+    size_t device_bytes = 0;
+    xsgb::Scratch s;
+    // tuned defaults
+    int plain_tile = 1024;
+    int batched_buckets = 4096;
+    int batched_blocks_per_sm = 4;
+    std::map<std::string, xsgb::BatchedGraph> graphs;
+    int sm_count = 0;
+    void *h_result = nullptr;                 // pinned: verification + error words
+    cudaStream_t last_stream = nullptr;       // stream of the last (async) run
+    int last_launches = 0;
+    // host-sample pipeline: two streams, two buffer sets
+    cudaStream_t pipe_stream[2] = {nullptr, nullptr};
+    cudaEvent_t pipe_event[2] = {nullptr, nullptr};
+    void *pipe_buf = nullptr;
+    size_t pipe_bytes = 0;
+};
+
+namespace xsgb {
+
+// error helpers (capi.cu)
+xs_status fail(xs_status s, const char *fmt, ...);
+xs_status cuda_fail(cudaError_t e, const char *what);
+#define XS_CUDA(call)                                            \
+    do {                                                         \
+        cudaError_t e__ = (call);                                \
+        if (e__ != cudaSuccess) return ::xsgb::cuda_fail(e__, #call); \
+    } while (0)
+
+// device memory owned by a context
+xs_status ctx_alloc(xs_ctx *ctx, void **p, size_t bytes);
+
+// derived-table builders (tables.cu)
+xs_status build_derived_tables(xs_ctx *ctx);
+
+// lookup launchers (lookup.cu).  Every launcher only enqueues on `st`.
+struct Outputs {
+    double *macro = nullptr;          // device, count*5, or null
+    unsigned char *max_idx = nullptr; // device, count, or null
+};
+struct SampleInput {
+    const double *energy = nullptr;   // device, or null: in-kernel LCG sampling
+    const int *mat = nullptr;
+};
+xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                       long count, int block, int tile, const SampleInput &in,
+                       const Outputs &out, int *launches);
+xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                         long count, int block, int buckets, const SampleInput &in,
+                         const Outputs &out, int *launches);
+xs_status launch_history(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                         int *launches);
+size_t batched_scratch_bytes(long count, int buckets);
+xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat);
+
+// host setup (setup_host.cu)
+void pick_mat_thresholds(double out[kMaterials]);
+
+}  // namespace xsgb
