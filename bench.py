@@ -272,7 +272,10 @@ def main():
     ctx = X.Context(inputs, problem, device=local)
     t_setup = time.perf_counter() - t_setup
     first = rank * N
-    stream = torch.cuda.current_stream()
+    # a non-default stream: its handle goes to the library and the events
+    # below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     kw = dict(kernel=args.kernel, arith=args.arith, first=first, count=N, stream=stream)
 
     # correctness of this very configuration (rank 0 holds lookups [0, N))

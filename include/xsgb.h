@@ -121,7 +121,8 @@ typedef struct {
     int energy_buckets;  /* BATCHED: energy buckets per material (power of 2); 0 = default */
     int checked;         /* 1: bounds-check every table index and report XS_ERR_DATA */
     int async;           /* 1: only enqueue (device or NULL outputs); finish with xs_ctx_sync */
-    void *stream;        /* cudaStream_t to order on; NULL = the context's own stream */
+    void *stream;        /* cudaStream_t to order on; NULL = the context's own stream
+                            (so the legacy default stream cannot be named here) */
 } xs_run_opts;
 
 /* Results of one run.  Output arrays may be NULL, host memory or device
