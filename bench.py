@@ -244,6 +244,8 @@ def main():
     ap.add_argument("--workload", default="large_unionized", choices=sorted(WORKLOADS))
     ap.add_argument("--kernel", default="plain", choices=["plain", "batched"])
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--tile", type=int, default=0, help="plain kernel: lookups per block tile")
+    ap.add_argument("--buckets", type=int, default=0, help="batched: energy buckets per material")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
@@ -276,7 +278,8 @@ def main():
     # below are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    kw = dict(kernel=args.kernel, arith=args.arith, first=first, count=N, stream=stream)
+    kw = dict(kernel=args.kernel, arith=args.arith, first=first, count=N, stream=stream,
+              tile=args.tile, buckets=args.buckets)
 
     # correctness of this very configuration (rank 0 holds lookups [0, N))
     r = ctx.run_event(**kw)
@@ -318,7 +321,7 @@ def main():
     hE, hM = pin((N,), torch.float64), pin((N,), torch.int32)
     ctx.sample_event(first, N, hE, hM)
     hmacro, hidx = pin((N, 5), torch.float64), pin((N,), torch.uint8)
-    ekw = dict(kernel=args.kernel, arith=args.arith)
+    ekw = dict(kernel=args.kernel, arith=args.arith, tile=args.tile, buckets=args.buckets)
     ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)  # warm
     e2e_t = []
     for _ in range(max(1, args.e2e_steps)):
@@ -345,6 +348,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the reference's own LCG problem generators)",
             "config": {"workload": args.workload, "kernel": args.kernel, "arith": args.arith,
+                       "tile": args.tile, "buckets": args.buckets,
                        "n_isotopes": inputs.n_isotopes, "n_gridpoints": inputs.n_gridpoints,
                        "grid": wl["grid"], "lookups_per_gpu": N,
                        "l2": "inputs larger than L2 (tables > 129 MB), no flush",

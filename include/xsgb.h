@@ -226,6 +226,27 @@ xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gba
  * JSON cache keyed by (device name, problem). */
 xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best);
 
+/* Allocation-free batched run.  It has no counterpart in the reference.
+ * The same lookups as xs_run_event with the BATCHED kernel, for callers that
+ * must not allocate device memory -- e.g. a host thread that drives other GPU
+ * work and must not stall it (cudaMalloc/cudaFree can synchronise the device),
+ * or a program whose memory manager owns the device budget.  Its sort buffers
+ * and counters live in one static device array of 6.5 MB that every GPU
+ * loading this library holds until exit; so it takes at most 524,288 lookups
+ * (count) and 4,096 energy buckets per call (larger values are rejected with
+ * XS_ERR_INVALID_ARGUMENT), and it calls no allocating routine.
+ * Outputs (macro_xs_out count*5, max_idx_out count) must be device memory or
+ * NULL; *verification (host) receives the un-modded sum; the call is ordered
+ * on `stream` (NULL: the context's stream) and returns when it is done.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race on it and must be serialised by the caller. */
+xs_status xs_run_event_batched_static(xs_ctx *ctx, long first, long count, int arith,
+                                      int energy_buckets, double *macro_xs_out,
+                                      unsigned char *max_idx_out, void *stream,
+                                      unsigned long long *verification);
+
 /* Full drop-in of the reference seam
  *   unsigned long long run_event_based_simulation(Inputs, SimulationData, int)
  * (openmp-threading/XSbench_header.h:117): creates a context on device 0,

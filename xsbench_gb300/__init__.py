@@ -103,6 +103,8 @@ _SIGNATURES = {
                         _P(RunResult)], C.c_int),
     "xs_autotune": ([C.c_void_p, C.c_char_p, _P(RunOpts)], C.c_int),
     "xs_run_event_based_simulation": ([Inputs, SimData, C.c_int, _P(C.c_ulonglong)], C.c_int),
+    "xs_run_event_batched_static": ([C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, _P(C.c_ulonglong)], C.c_int),
 }
 
 _lib = None
@@ -322,6 +324,22 @@ class Context:
         r = RunResult()
         _check(lib().xs_run_history(self._h, C.byref(o), C.byref(r)), "xs_run_history")
         return Result(r)
+
+    def run_event_batched_static(self, first: int, count: int, arith="fast", buckets=0,
+                                 macro_out=None, max_idx_out=None, stream=None) -> int:
+        """Batched lookups with no device allocation (at most 524,288 per call;
+        outputs on the device or None); returns the un-modded verification sum."""
+        v = C.c_ulonglong()
+        pm, dm = _addr(macro_out)
+        pi, di = _addr(max_idx_out)
+        if (pm and not dm) or (pi and not di):
+            raise ValueError("outputs must be device tensors")
+        a = {"fast": ARITH_FAST, "exact": ARITH_EXACT}.get(arith, arith)
+        s = None if stream is None else C.c_void_p(stream if isinstance(stream, int) else stream.cuda_stream)
+        _check(lib().xs_run_event_batched_static(self._h, int(first), int(count), int(a),
+                                                 int(buckets), pm, pi, s, C.byref(v)),
+               "xs_run_event_batched_static")
+        return int(v.value)
 
     def sync(self) -> Result:
         r = RunResult()

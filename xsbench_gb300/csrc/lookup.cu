@@ -248,6 +248,28 @@ static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int ch
     return XS_OK;
 }
 
+// The batched pipeline over caller-provided scratch: the same four kernels
+// as enqueue_batched, launched directly (no graph), for the entry point whose
+// scratch is a static device array (static_scratch.cu).
+xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                             int nb_log2, const BatchedScratch &b, const Outputs &out)
+{
+    const unsigned blocks =
+        (unsigned)((count + (long)kBlock * kSortLpt - 1) / ((long)kBlock * kSortLpt));
+    k_sort_pass<false, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr,
+                                                          nullptr, b.offs, b.sE, b.sid, b.error);
+    XS_CUDA(cudaGetLastError());
+    k_sort_scan<<<1, kScanThreads, 0, st>>>(b.offs, nb_log2, b.seg, b.cnt);
+    XS_CUDA(cudaGetLastError());
+    k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr,
+                                                         nullptr, b.offs, b.sE, b.sid, b.error);
+    XS_CUDA(cudaGetLastError());
+    XS_CUDA(batched_fn(ctx->t.grid_type)(ctx->t, st, arith, 0, ctx->sm_count * ctx->batched_blocks_per_sm,
+                                         b.seg, b.cnt, b.sE, b.sid, b.queue, out.macro,
+                                         out.max_idx, b.verification, b.error));
+    return XS_OK;
+}
+
 xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                          long count, int block, int buckets, const SampleInput &in,
                          const Outputs &out, int *launches)

@@ -125,6 +125,19 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
 xs_status launch_history(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
                          int *launches);
 size_t batched_scratch_bytes(long count, int buckets);
+// Explicit device buffers of one batched run (every pointer into caller memory).
+struct BatchedScratch {
+    unsigned long long *verification;
+    int *error;
+    unsigned int *queue;
+    int *offs;   // [12 << nb_log2]
+    int *seg;    // [13]
+    int *cnt;    // [12]
+    double *sE;  // [count + 384]
+    int *sid;    // [count + 384]
+};
+xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                             int nb_log2, const BatchedScratch &b, const Outputs &out);
 xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat);
 
 // host setup (setup_host.cu)
