@@ -245,6 +245,8 @@ def main():
     ap.add_argument("--kernel", default="plain", choices=["plain", "batched"])
     ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
     ap.add_argument("--tile", type=int, default=0, help="plain kernel: lookups per block tile")
+    ap.add_argument("--gridpoints", type=int, default=0,
+                    help="override gridpoints per nuclide (a smaller case of the workload, for profiling)")
     ap.add_argument("--buckets", type=int, default=0, help="batched: energy buckets per material")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -267,6 +269,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     wl = dict(WORKLOADS[args.workload])
+    if args.gridpoints:
+        wl["gridpoints"] = args.gridpoints
     inputs = X.make_inputs(method="event", **wl)
     N = inputs.lookups
     t_setup = time.perf_counter()
@@ -283,7 +287,8 @@ def main():
 
     # correctness of this very configuration (rank 0 holds lookups [0, N))
     r = ctx.run_event(**kw)
-    expected = X.EXPECTED_HASH.get(("event", wl["size"].lower()))
+    # the published hash holds for the workload as defined (not for a resized one)
+    expected = None if args.gridpoints else X.EXPECTED_HASH.get(("event", wl["size"].lower()))
     hash_ok = (expected is None or rank != 0 or N != 17000000 or r.hash == expected)
     for _ in range(args.warmup):
         ctx.run_event(async_=True, **kw)

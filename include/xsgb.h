@@ -210,16 +210,28 @@ xs_status xs_lookup_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *
  * [first, first+count) of opts (count <= 0: inputs.particles). */
 xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *result);
 
-/* Adjoint of the lookup.  For upstream gradients gbar (count*5, the
- * derivative of a scalar loss with respect to each macro_xs of lookups
- * [first, first+count)) it accumulates
- *   d_concs  (12*max_num_nucs)            += dL/dconcs
- *   d_xs     (n_isotopes*n_gridpoints*5)  += dL/d(tabulated xs channels)
- * and writes d_energy (count) = dL/d(sampled energy).  Any output may be NULL.
- * The search indices are recomputed, not stored.  The sums are deterministic. */
+/* Adjoint of the lookup (no reference counterpart: the reference has no
+ * derivatives; it differentiates calculate_macro_xs, Simulation.c:241-375).
+ * For upstream gradients gbar (count*5: dL/dmacro_xs of lookups
+ * [first, first+count) for a scalar loss L) it computes
+ *   d_energy (count)                      =  dL/d(sampled energy)
+ *   d_concs  (12*max_num_nucs)           +=  dL/dconcs
+ *   d_xs     (n_isotopes*n_gridpoints*5) +=  dL/d(tabulated xs: total, elastic,
+ *                                            absorbtion, fission, nu_fission)
+ * and, when macro_xs_out is non-NULL, the forward macro_xs (count*5).  Any
+ * output may be NULL.  The search indices are recomputed, not stored.  Every
+ * sum runs in a fixed order over a deterministic (material, energy, index)
+ * sort, so the results are bit-reproducible.  Arrays may be host or device
+ * memory (all of one kind). */
 xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gbar,
-                         double *d_concs, double *d_xs, double *d_energy,
-                         xs_run_result *result);
+                         double *macro_xs_out, double *d_concs, double *d_xs,
+                         double *d_energy, xs_run_result *result);
+
+/* The same for caller-supplied samples (energy, mat: n entries). */
+xs_status xs_adjoint_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
+                             const int *mat, long n, const double *gbar, double *macro_xs_out,
+                             double *d_concs, double *d_xs, double *d_energy,
+                             xs_run_result *result);
 
 /* Times the kernel shapes on this context and keeps the fastest as its
  * defaults; with cache_path non-NULL the choice is read from / merged into a

@@ -100,7 +100,9 @@ _SIGNATURES = {
     "xs_run_history": ([C.c_void_p, _P(RunOpts), _P(RunResult)], C.c_int),
     "xs_sample_event": ([C.c_void_p, C.c_long, C.c_long, C.c_void_p, C.c_void_p], C.c_int),
     "xs_run_adjoint": ([C.c_void_p, _P(RunOpts), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                        _P(RunResult)], C.c_int),
+                        C.c_void_p, _P(RunResult)], C.c_int),
+    "xs_adjoint_samples": ([C.c_void_p, _P(RunOpts), C.c_void_p, C.c_void_p, C.c_long, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _P(RunResult)], C.c_int),
     "xs_autotune": ([C.c_void_p, C.c_char_p, _P(RunOpts)], C.c_int),
     "xs_run_event_based_simulation": ([Inputs, SimData, C.c_int, _P(C.c_ulonglong)], C.c_int),
     "xs_run_event_batched_static": ([C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int, C.c_void_p,
@@ -340,6 +342,25 @@ class Context:
                                                  int(buckets), pm, pi, s, C.byref(v)),
                "xs_run_event_batched_static")
         return int(v.value)
+
+    def adjoint(self, gbar, energy=None, mat=None, macro_out=None, d_concs=None, d_xs=None,
+                d_energy=None, **kw) -> Result:
+        """Gradients of L = sum(gbar * macro_xs): d_energy is written, d_concs
+        (12 x max_num_nucs) and d_xs (n_isotopes x n_gridpoints x 5) are added
+        to.  Lookups are [first, first+count) of the event batch, or the
+        caller's (energy, mat) samples."""
+        o = _opts(**kw)
+        r = RunResult()
+        a = [_addr(x)[0] for x in (gbar, macro_out, d_concs, d_xs, d_energy)]
+        if energy is None:
+            _check(lib().xs_run_adjoint(self._h, C.byref(o), *a, C.byref(r)), "xs_run_adjoint")
+        else:
+            n = int(energy.shape[0])
+            pe, _ = _addr(energy)
+            pm, _ = _addr(mat)
+            _check(lib().xs_adjoint_samples(self._h, C.byref(o), pe, pm, n, *a, C.byref(r)),
+                   "xs_adjoint_samples")
+        return Result(r)
 
     def sync(self) -> Result:
         r = RunResult()

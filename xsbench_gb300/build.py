@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libxsgb.so")
 EXE_PATH = os.path.join(LIB_DIR, "xsgb")
 
 CU_SOURCES = ["capi.cu", "setup_host.cu", "tables.cu", "lookup.cu", "lookup_unionized.cu",
-              "lookup_nuclide.cu", "lookup_hash.cu", "static_scratch.cu"]
+              "lookup_nuclide.cu", "lookup_hash.cu", "static_scratch.cu", "adjoint.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -57,6 +57,7 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> 
              "-Xcompiler", "-Wall", "-I", os.path.join(ROOT, "include")]
     if ptxas_v:
         flags += ["-Xptxas", "-v"]
+    flags += os.environ.get("XSGB_NVCC_FLAGS", "").split()
     jobs = []
     objs = []
     for src in CU_SOURCES:

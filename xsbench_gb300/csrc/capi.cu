@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "device_common.cuh"
 
@@ -35,7 +36,10 @@ xs_status cuda_fail(cudaError_t e, const char *what)
 xs_status ctx_alloc(xs_ctx *ctx, void **p, size_t bytes)
 {
     *p = nullptr;
-    if (bytes == 0) bytes = 16;
+    // whole 256-byte units, so a 16-byte-rounded bulk prefetch of the last
+    // entries stays inside the allocation
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (bytes == 0) bytes = 256;
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -88,6 +92,34 @@ static xs_status ensure_stage(xs_ctx *ctx, size_t bytes)
     ctx->s.stage_bytes = bytes;
     ctx->device_bytes += bytes;
     return XS_OK;
+}
+
+static xs_status ensure_plain(xs_ctx *ctx, size_t bytes)
+{
+    if (ctx->s.plain_bytes >= bytes) return XS_OK;
+    if (ctx->s.plain_buf) {
+        cudaFree(ctx->s.plain_buf);
+        ctx->device_bytes -= ctx->s.plain_bytes;
+        ctx->s.plain_buf = nullptr;
+        ctx->s.plain_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&ctx->s.plain_buf, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(XS_ERR_OUT_OF_MEMORY, "overflow queues of %zu bytes", bytes);
+    }
+    ctx->s.plain_bytes = bytes;
+    ctx->device_bytes += bytes;
+    return XS_OK;
+}
+
+// Plain runs of more than a few tiles send each tile's partial chunks to the
+// overflow queues (two more launches); short runs keep them in the tile.  On
+// the nuclide grid the queued lookups cost more (long unsorted searches in
+// fewer resident warps) than the idle lanes they save, so it keeps them too.
+static bool use_overflow(const xs_ctx *ctx, long count, int tile)
+{
+    return ctx->t.grid_type != XS_NUCLIDE && count > 8L * tile;
 }
 
 static xs_status resolve(const xs_ctx *ctx, const xs_run_opts *o, long total, xs_run_opts *r)
@@ -173,6 +205,8 @@ void xs_ctx_destroy(xs_ctx *ctx)
     if (ctx->s.sort_buf) cudaFree(ctx->s.sort_buf);
     if (ctx->s.stage) cudaFree(ctx->s.stage);
     if (ctx->pipe_buf) cudaFree(ctx->pipe_buf);
+    if (ctx->s.plain_buf) cudaFree(ctx->s.plain_buf);
+    if (ctx->s.adj_buf) cudaFree(ctx->s.adj_buf);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -281,8 +315,39 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
     if (s != XS_OK) return s;
     Tables &t = ctx->t;
     t.max_nucs = sd->max_num_nucs;
+    for (int m = 0; m < kMaterials; m++) {
+        int lo = (int)in->n_isotopes - 1, hi = 0;
+        for (int j = 0; j < sd->num_nucs[m]; j++) {
+            const int nuc = sd->mats[m * sd->max_num_nucs + j];
+            lo = nuc < lo ? nuc : lo;
+            hi = nuc > hi ? nuc : hi;
+        }
+        if (lo > hi) lo = hi = 0;
+        t.mat_lo[m] = lo;
+        t.mat_hi[m] = hi;
+    }
+    {   // (material, position) pairs, and for each nuclide the pairs holding it
+        t.pair_base[0] = 0;
+        for (int m = 0; m < kMaterials; m++) t.pair_base[m + 1] = t.pair_base[m] + sd->num_nucs[m];
+        std::vector<int> off((size_t)in->n_isotopes + 1, 0), pairs((size_t)t.pair_base[kMaterials] + 1, 0);
+        for (int m = 0; m < kMaterials; m++)
+            for (int j = 0; j < sd->num_nucs[m]; j++) off[(size_t)sd->mats[m * sd->max_num_nucs + j] + 1]++;
+        for (long n = 0; n < in->n_isotopes; n++) off[(size_t)n + 1] += off[(size_t)n];
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        for (int m = 0; m < kMaterials; m++)
+            for (int j = 0; j < sd->num_nucs[m]; j++) {
+                const int nuc = sd->mats[m * sd->max_num_nucs + j];
+                pairs[(size_t)fill[(size_t)nuc]++] = m * sd->max_num_nucs + j;
+            }
+        if (s == XS_OK) s = upload(ctx, off.data(), off.size(), &t.inv_off);
+        if (s == XS_OK) s = upload(ctx, pairs.data(), pairs.size(), &t.inv_pair);
+        if (s == XS_OK) {  // the host vectors go out of scope
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamSynchronize");
+        }
+    }
     const long n_pts = in->n_isotopes * in->n_gridpoints;
-    s = upload(ctx, sd->num_nucs, kMaterials, &t.num_nucs);
+    if (s == XS_OK) s = upload(ctx, sd->num_nucs, kMaterials, &t.num_nucs);
     if (s == XS_OK) s = upload(ctx, sd->mats, (size_t)sd->length_mats, &t.mats);
     if (s == XS_OK) s = upload(ctx, sd->concs, (size_t)sd->length_concs, &t.concs);
     if (s == XS_OK) s = upload(ctx, sd->nuclide_grid, (size_t)n_pts, &t.grid);
@@ -397,9 +462,17 @@ static xs_status run_once(xs_ctx *ctx, const xs_run_opts &o, const SampleInput &
     XS_CUDA(cudaEventRecord(ctx->ev0, st));
     int launches = 0;
     xs_status s;
-    if (o.kernel == XS_KERNEL_PLAIN)
-        s = launch_plain(ctx, st, o.arith, o.checked, o.first, n, 256, o.tile_lookups, in, out, &launches);
-    else
+    if (o.kernel == XS_KERNEL_PLAIN) {
+        PlainScratch ps;
+        const PlainScratch *psp = nullptr;
+        if (use_overflow(ctx, n, o.tile_lookups)) {
+            s = ensure_plain(ctx, plain_scratch_bytes(n, o.tile_lookups));
+            if (s != XS_OK) return s;
+            ps = carve_plain_scratch(ctx->s.plain_buf, n, o.tile_lookups);
+            psp = &ps;
+        }
+        s = launch_plain(ctx, st, o.arith, o.checked, o.first, n, o.tile_lookups, in, out, psp, &launches);
+    } else
         s = launch_batched(ctx, st, o.arith, o.checked, o.first, n, 256, o.energy_buckets, in, out, &launches);
     if (s != XS_OK) return s;
     XS_CUDA(cudaEventRecord(ctx->ev1, st));
@@ -439,7 +512,10 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
 {
     const long chunk = o.tile_lookups > 0 && o.kernel == XS_KERNEL_PLAIN ? std::max<long>(1L << 20, o.tile_lookups) : (1L << 21);
     const size_t per = 8 + 4 + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
-    const size_t need = 2 * ((size_t)chunk * per + 1024);
+    const size_t io_bytes = ((size_t)chunk * per + 1023) & ~(size_t)255;
+    const bool ovf = o.kernel == XS_KERNEL_PLAIN && use_overflow(ctx, chunk, o.tile_lookups);
+    const size_t slot = io_bytes + (ovf ? plain_scratch_bytes(chunk, o.tile_lookups) : 0);
+    const size_t need = 2 * slot;
     if (ctx->pipe_bytes < need) {
         if (ctx->pipe_buf) {
             cudaFree(ctx->pipe_buf);
@@ -467,7 +543,7 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         const int w = (int)(k & 1);
         cudaStream_t st = ctx->pipe_stream[w];
         const long m = std::min(chunk, n - c0);
-        char *b = (char *)ctx->pipe_buf + (size_t)w * (need / 2);
+        char *b = (char *)ctx->pipe_buf + (size_t)w * slot;
         double *dE = (double *)b;
         int *dM = (int *)(b + (size_t)chunk * 8);
         double *dMacro = macro_out ? (double *)(b + (size_t)chunk * 12) : nullptr;
@@ -481,9 +557,12 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         out.macro = dMacro;
         out.max_idx = dIdx;
         xs_status s;
-        if (o.kernel == XS_KERNEL_PLAIN)
-            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, 256, o.tile_lookups, in, out, &launches);
-        else
+        if (o.kernel == XS_KERNEL_PLAIN) {
+            PlainScratch ps;
+            if (ovf) ps = carve_plain_scratch(b + io_bytes, chunk, o.tile_lookups);
+            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, in, out,
+                             ovf && use_overflow(ctx, m, o.tile_lookups) ? &ps : nullptr, &launches);
+        } else
             s = launch_batched(ctx, st, o.arith, o.checked, 0, m, 256, o.energy_buckets, in, out, &launches);
         if (s != XS_OK) return s;
         if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));
@@ -575,11 +654,111 @@ xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *re
     return s;
 }
 
-xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gbar,
-                         double *d_concs, double *d_xs, double *d_energy, xs_run_result *result)
+// The adjoint for LCG-sampled (in.energy == NULL) or caller-sampled lookups.
+static xs_status adjoint_common(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
+                                const int *mat, long n_samples, const double *gbar,
+                                double *macro_out, double *d_concs, double *d_xs,
+                                double *d_energy, xs_run_result *result)
 {
-    (void)ctx; (void)opts; (void)gbar; (void)d_concs; (void)d_xs; (void)d_energy; (void)result;
-    return fail(XS_ERR_UNSUPPORTED, "adjoint is not built in this version");
+    if (!ctx) return fail(XS_ERR_INVALID_ARGUMENT, "adjoint: NULL context");
+    if (!gbar) return fail(XS_ERR_INVALID_ARGUMENT, "adjoint: gbar is NULL");
+    XS_CUDA(cudaSetDevice(ctx->device));
+    xs_run_opts o;
+    const bool samples = energy != nullptr;
+    xs_status s = resolve(ctx, opts, samples ? n_samples : (long)ctx->inputs.lookups, &o);
+    if (s != XS_OK) return s;
+    if (samples) {
+        o.first = 0;
+        o.count = n_samples;
+    }
+    const long n = o.count;
+    const Tables &t = ctx->t;
+    const size_t nconc = (size_t)kMaterials * t.max_nucs, nxs = (size_t)t.n_iso * t.n_gp * 5;
+    const void *ptrs[7] = {energy, mat, gbar, macro_out, d_concs, d_xs, d_energy};
+    int ndev = 0, nhost = 0;
+    for (const void *p : ptrs) {
+        if (!p) continue;
+        if (is_device_pointer(p)) ndev++; else nhost++;
+    }
+    if (ndev && nhost) return fail(XS_ERR_INVALID_ARGUMENT, "adjoint: arrays must be all host or all device memory");
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : ctx->stream;
+    SampleInput in;
+    const double *g_dev = gbar;
+    double *m_dev = macro_out, *c_dev = d_concs, *x_dev = d_xs, *e_dev = d_energy;
+    if (nhost) {
+        // one staging block: samples, gbar, outputs, zeroed gradient sums
+        const size_t bytes = (samples ? (size_t)n * 12 : 0) + (size_t)n * 40 +
+                             (macro_out ? (size_t)n * 40 : 0) + (d_energy ? (size_t)n * 8 : 0) +
+                             (d_concs ? nconc * 8 : 0) + (d_xs ? nxs * 8 : 0) + 1024;
+        s = ensure_stage(ctx, bytes);
+        if (s != XS_OK) return s;
+        char *b = (char *)ctx->s.stage;
+        auto take = [&](size_t sz) { char *r = b; b += (sz + 255) & ~(size_t)255; return r; };
+        if (samples) {
+            double *dE = (double *)take((size_t)n * 8);
+            int *dM = (int *)take((size_t)n * 4);
+            XS_CUDA(cudaMemcpyAsync(dE, energy, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+            XS_CUDA(cudaMemcpyAsync(dM, mat, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+            in.energy = dE;
+            in.mat = dM;
+        }
+        double *dg = (double *)take((size_t)n * 40);
+        XS_CUDA(cudaMemcpyAsync(dg, gbar, (size_t)n * 40, cudaMemcpyHostToDevice, st));
+        g_dev = dg;
+        m_dev = macro_out ? (double *)take((size_t)n * 40) : nullptr;
+        e_dev = d_energy ? (double *)take((size_t)n * 8) : nullptr;
+        c_dev = d_concs ? (double *)take(nconc * 8) : nullptr;
+        x_dev = d_xs ? (double *)take(nxs * 8) : nullptr;
+        if (c_dev) XS_CUDA(cudaMemsetAsync(c_dev, 0, nconc * 8, st));
+        if (x_dev) XS_CUDA(cudaMemsetAsync(x_dev, 0, nxs * 8, st));
+    } else if (samples) {
+        in.energy = energy;
+        in.mat = mat;
+    }
+    XS_CUDA(cudaMemsetAsync(ctx->s.verification, 0, 8, st));
+    XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, st));
+    XS_CUDA(cudaEventRecord(ctx->ev0, st));
+    int launches = 0;
+    s = launch_adjoint(ctx, st, o.first, n, in, g_dev, m_dev, c_dev, x_dev, e_dev, &launches);
+    if (s != XS_OK) return s;
+    XS_CUDA(cudaEventRecord(ctx->ev1, st));
+    std::vector<double> hc, hx;
+    if (nhost) {
+        if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out, m_dev, (size_t)n * 40, cudaMemcpyDeviceToHost, st));
+        if (d_energy) XS_CUDA(cudaMemcpyAsync(d_energy, e_dev, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+        if (d_concs) {
+            hc.resize(nconc);
+            XS_CUDA(cudaMemcpyAsync(hc.data(), c_dev, nconc * 8, cudaMemcpyDeviceToHost, st));
+        }
+        if (d_xs) {
+            hx.resize(nxs);
+            XS_CUDA(cudaMemcpyAsync(hx.data(), x_dev, nxs * 8, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    s = read_back(ctx, st, result);
+    if (result) result->kernel_launches = launches;
+    if (s != XS_OK) return s;
+    for (size_t i = 0; i < hc.size(); i++) d_concs[i] += hc[i];
+    for (size_t i = 0; i < hx.size(); i++) d_xs[i] += hx[i];
+    return XS_OK;
+}
+
+xs_status xs_run_adjoint(xs_ctx *ctx, const xs_run_opts *opts, const double *gbar,
+                         double *macro_xs_out, double *d_concs, double *d_xs, double *d_energy,
+                         xs_run_result *result)
+{
+    return adjoint_common(ctx, opts, nullptr, nullptr, 0, gbar, macro_xs_out, d_concs, d_xs,
+                          d_energy, result);
+}
+
+xs_status xs_adjoint_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
+                             const int *mat, long n, const double *gbar, double *macro_xs_out,
+                             double *d_concs, double *d_xs, double *d_energy,
+                             xs_run_result *result)
+{
+    if (!energy || !mat || n <= 0) return fail(XS_ERR_INVALID_ARGUMENT, "xs_adjoint_samples: need energy, mat and n > 0");
+    return adjoint_common(ctx, opts, energy, mat, n, gbar, macro_xs_out, d_concs, d_xs, d_energy,
+                          result);
 }
 
 xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best)

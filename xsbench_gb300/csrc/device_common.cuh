@@ -196,21 +196,51 @@ __device__ __forceinline__ long interval_hash(const Tables &t, long bin, int nuc
     return (lower == n_gp - 1) ? lower - 1 : lower;
 }
 
-// --------------------------------------------------------- interpolation ---
-// FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record.
-__device__ __forceinline__ void accumulate_fast(const Tables &t, int nuc, long k, double E,
-                                                double conc, double macro[5])
+// ------------------------------------------------------------- prefetch ---
+// TMA bulk prefetch of [p, p+bytes) into L2; p 16-byte aligned, bytes a
+// multiple of 16 (one instruction per 96-byte record or index-row span).
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
 {
-    const double2 *r = t.records + ((long)nuc * (t.n_gp - 1) + k) * 6;
-    const double2 r0 = ldg(r + 0), r1 = ldg(r + 1), r2 = ldg(r + 2);
-    const double2 r3 = ldg(r + 3), r4 = ldg(r + 4), r5 = ldg(r + 5);
-    const double d = r0.x - E;
-    macro[0] = fma(fma(-d, r3.x, r0.y), conc, macro[0]);
-    macro[1] = fma(fma(-d, r3.y, r1.x), conc, macro[1]);
-    macro[2] = fma(fma(-d, r4.x, r1.y), conc, macro[2]);
-    macro[3] = fma(fma(-d, r4.y, r2.x), conc, macro[3]);
-    macro[4] = fma(fma(-d, r5.x, r2.y), conc, macro[4]);
-    (void)r5;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// --------------------------------------------------------- interpolation ---
+// 32-byte read-only load that does not allocate in L1 (the records are
+// streamed; the material tables and index rows keep L1 to themselves).
+__device__ __forceinline__ void ld_v4(const double *p, double &a, double &b, double &c, double &d)
+{
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0,%1,%2,%3}, [%4];"
+                 : "=d"(a), "=d"(b), "=d"(c), "=d"(d)
+                 : "l"(p));
+}
+
+// FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record, read
+// with three 32-byte loads (a record is three aligned sectors).
+template <bool DE = false>
+__device__ __forceinline__ void accumulate_fast(const Tables &t, int nuc, long k, double E,
+                                                double conc, double macro[5], double *S = nullptr)
+{
+    const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * 6);
+    double e_hi, h0, h1, h2, h3, h4, s0, s1, s2, s3, s4, e_lo;
+    ld_v4(r, e_hi, h0, h1, h2);
+    ld_v4(r + 4, h3, h4, s0, s1);
+    ld_v4(r + 8, s2, s3, s4, e_lo);
+    (void)e_lo;
+    const double d = e_hi - E;
+    macro[0] = fma(fma(-d, s0, h0), conc, macro[0]);
+    macro[1] = fma(fma(-d, s1, h1), conc, macro[1]);
+    macro[2] = fma(fma(-d, s2, h2), conc, macro[2]);
+    macro[3] = fma(fma(-d, s3, h3), conc, macro[3]);
+    macro[4] = fma(fma(-d, s4, h4), conc, macro[4]);
+    if (DE) {  // d macro / dE = sum over nuclides of conc * slope
+        S[0] = fma(conc, s0, S[0]);
+        S[1] = fma(conc, s1, S[1]);
+        S[2] = fma(conc, s2, S[2]);
+        S[3] = fma(conc, s3, S[3]);
+        S[4] = fma(conc, s4, S[4]);
+    }
 }
 
 // EXACT: the reference's operations in its order (Simulation.c:304-322,
@@ -245,17 +275,93 @@ __device__ __forceinline__ int argmax5(const double m[5])
     return arg;
 }
 
+// Address of the 96 bytes a lookup reads for interval k of nuclide nuc.
+template <int ARITH>
+__device__ __forceinline__ const void *interval_bytes(const Tables &t, int nuc, long k)
+{
+    if (ARITH == XS_ARITH_EXACT) return t.grid + (long)nuc * t.n_gp + k;
+    return t.records + ((long)nuc * (t.n_gp - 1) + k) * 6;
+}
+
+// UNIONIZED nuclide loop, software-pipelined: the index entry of nuclide j+2P
+// is loaded and the 96-byte interval of nuclide j+P is prefetched into L2 while
+// nuclide j is interpolated, so a lane keeps three gathers in flight instead
+// of waiting on each dependent pair.  Accumulation order is the reference's.
+template <int ARITH, bool CHECKED, bool DE>
+__device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, int mat, int n,
+                                                   const int *mrow, const double *crow,
+                                                   double macro[5], int *err, double *S)
+{
+    constexpr int P = 2;
+    const long row = union_row(t, E);
+    const int *irow = t.index_grid + row * t.n_iso;
+    {
+        // the material's span of the index row, 16-byte aligned
+        const uintptr_t a = (uintptr_t)(irow + t.mat_lo[mat]) & ~(uintptr_t)15;
+        const uintptr_t b = ((uintptr_t)(irow + t.mat_hi[mat] + 1) + 15) & ~(uintptr_t)15;
+        prefetch_l2((const void *)a, (unsigned)(b - a));
+    }
+    const long top = t.n_gp - 1;
+    int kr[2 * P];
+#pragma unroll
+    for (int q = 0; q < 2 * P; q++) kr[q] = (q < n) ? ldg(&irow[ldg(&mrow[q])]) : 0;
+#pragma unroll
+    for (int q = 0; q < P; q++)
+        if (q < n) {
+            long k = kr[q];
+            if (CHECKED && (k < 0 || k > top)) k = 0;
+            prefetch_l2(interval_bytes<ARITH>(t, ldg(&mrow[q]), k == top ? k - 1 : k), 96);
+        }
+    for (int j0 = 0; j0 < n; j0 += 2 * P) {
+#pragma unroll
+        for (int q = 0; q < 2 * P; q++) {
+            const int j = j0 + q;
+            if (j < n) {
+                long k = kr[q];
+                if (CHECKED && (k < 0 || k > top)) {
+                    report(err, XS_ERR_DATA, row, ldg(&mrow[j]));
+                    k = 0;
+                }
+                if (k == top) k -= 1;
+                const int jn = j + 2 * P;
+                if (jn < n) kr[q] = ldg(&irow[ldg(&mrow[jn])]);
+                const int jp = j + P;
+                if (jp < n) {
+                    long kp = kr[(q + P) % (2 * P)];
+                    if (CHECKED && (kp < 0 || kp > top)) kp = 0;
+                    prefetch_l2(interval_bytes<ARITH>(t, ldg(&mrow[jp]), kp == top ? kp - 1 : kp), 96);
+                }
+                const int nuc = ldg(&mrow[j]);
+                const double conc = ldg(&crow[j]);
+                if (ARITH == XS_ARITH_EXACT)
+                    accumulate_exact(t, nuc, k, E, conc, macro);
+                else
+                    accumulate_fast<DE>(t, nuc, k, E, conc, macro, S);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------ one lookup ---
 // calculate_macro_xs (Simulation.c:326-375) for one (E, mat).
-template <int GRID, int ARITH, bool CHECKED>
+// With DE, S[5] receives d macro_xs / dE (the adjoint's energy derivative).
+template <int GRID, int ARITH, bool CHECKED, bool DE = false>
 __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, double macro[5],
-                                         int *err)
+                                         int *err, double *S = nullptr)
 {
 #pragma unroll
     for (int c = 0; c < 5; c++) macro[c] = 0.0;
+    if (DE) {
+#pragma unroll
+        for (int c = 0; c < 5; c++) S[c] = 0.0;
+    }
     const int n = ldg(&t.num_nucs[mat]);
     const int *mrow = t.mats + mat * t.max_nucs;
     const double *crow = t.concs + mat * t.max_nucs;
+    if (GRID == XS_UNIONIZED) {
+        macro_xs_unionized<ARITH, CHECKED, DE>(t, E, mat, n, mrow, crow, macro, err, S);
+        return;
+    }
     long row = 0;
     long long q = 0;
     const bool keyed = !(E != E);   // NaN energies use the double-compare path
@@ -300,7 +406,7 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
         if (ARITH == XS_ARITH_EXACT)
             accumulate_exact(t, nuc, k, E, conc, macro);
         else
-            accumulate_fast(t, nuc, k, E, conc, macro);
+            accumulate_fast<DE>(t, nuc, k, E, conc, macro, S);
     }
 }
 

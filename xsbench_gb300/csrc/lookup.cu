@@ -165,12 +165,8 @@ static int ilog2(int x)
     return l;
 }
 
-typedef cudaError_t (*PlainFn)(const Tables &, cudaStream_t, int, int, bool, long, long, int,
-                               const double *, const int *, double *, unsigned char *,
-                               unsigned long long *, int *);
-typedef cudaError_t (*BatchedFn)(const Tables &, cudaStream_t, int, int, int, const int *,
-                                 const int *, const double *, const int *, unsigned int *,
-                                 double *, unsigned char *, unsigned long long *, int *);
+typedef cudaError_t (*PlainFn)(const Tables &, cudaStream_t, int, int, bool, const PlainArgs &);
+typedef cudaError_t (*ListFn)(const Tables &, cudaStream_t, int, int, int, const ListArgs &);
 typedef cudaError_t (*HistoryFn)(const Tables &, cudaStream_t, int, long, long, int,
                                  unsigned long long *, int *);
 
@@ -178,26 +174,100 @@ static PlainFn plain_fn(int g)
 {
     return g == XS_UNIONIZED ? unionized_plain : g == XS_NUCLIDE ? nuclide_plain : hash_plain;
 }
-static BatchedFn batched_fn(int g)
+static ListFn list_fn(int g)
 {
-    return g == XS_UNIONIZED ? unionized_batched : g == XS_NUCLIDE ? nuclide_batched : hash_batched;
+    return g == XS_UNIONIZED ? unionized_list : g == XS_NUCLIDE ? nuclide_list : hash_list;
 }
 static HistoryFn history_fn(int g)
 {
     return g == XS_UNIONIZED ? unionized_history : g == XS_NUCLIDE ? nuclide_history : hash_history;
 }
 
-xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                       long count, int block, int tile, const SampleInput &in,
-                       const Outputs &out, int *launches)
+// Packed chunk layout of the overflow queues: material m's entries sit at
+// [m*cap, m*cap + cnt[m]); its chunks start at the running sum of the
+// 32-rounded counts.
+__global__ void k_overflow_seg(const int *cnt, int cap, int *seg_v, int *base)
 {
-    (void)block;
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int m = 0; m < kMaterials; m++) {
+            seg_v[m] = s;
+            base[m] = m * cap;
+            s += (cnt[m] + 31) & ~31;
+        }
+        seg_v[kMaterials] = s;
+    }
+}
+
+static int overflow_cap(long count, int tile)
+{
+    const long tiles = (count + tile - 1) / tile;
+    return (int)(((tiles * 31) + 31) & ~31L);
+}
+
+size_t plain_scratch_bytes(long count, int tile)
+{
+    const size_t cap = (size_t)overflow_cap(count, tile);
+    return 1024 + (size_t)kMaterials * cap * 12 + 256;
+}
+
+PlainScratch carve_plain_scratch(void *buf, long count, int tile)
+{
+    PlainScratch p;
+    char *b = (char *)buf;
+    p.cap = overflow_cap(count, tile);
+    p.cnt = (int *)b;            // [12]
+    p.seg_v = (int *)(b + 64);   // [13]
+    p.base = (int *)(b + 128);   // [12]
+    p.queue = (unsigned int *)(b + 192);
+    p.E = (double *)(b + 1024);
+    p.id = (int *)(b + 1024 + (size_t)kMaterials * p.cap * 8);
+    return p;
+}
+
+xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                       long count, int tile, const SampleInput &in, const Outputs &out,
+                       const PlainScratch *ps, int *launches)
+{
     if (tile < kBlock || tile % kBlock) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d must be a multiple of %d", tile, kBlock);
     if (tile > 8192) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d above 8192", tile);
-    XS_CUDA(plain_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, in.energy != nullptr, first,
-                                       count, tile, in.energy, in.mat, out.macro, out.max_idx,
-                                       ctx->s.verification, ctx->s.error));
+    PlainArgs a;
+    a.first = first;
+    a.count = count;
+    a.tile = tile;
+    a.in_E = in.energy;
+    a.in_mat = in.mat;
+    a.out_macro = out.macro;
+    a.out_idx = out.max_idx;
+    a.verif = ctx->s.verification;
+    a.err = ctx->s.error;
+    a.ovf_cnt = ps ? ps->cnt : nullptr;
+    a.ovf_E = ps ? ps->E : nullptr;
+    a.ovf_id = ps ? ps->id : nullptr;
+    a.ovf_cap = ps ? ps->cap : 0;
+    if (ps) {
+        XS_CUDA(cudaMemsetAsync(ps->cnt, 0, 256, st));  // counts, layout, queue
+    }
+    XS_CUDA(plain_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, in.energy != nullptr, a));
     if (launches) *launches += 1;
+    if (ps) {
+        k_overflow_seg<<<1, 32, 0, st>>>(ps->cnt, ps->cap, ps->seg_v, ps->base);
+        XS_CUDA(cudaGetLastError());
+        ListArgs l;
+        l.seg_v = ps->seg_v;
+        l.cnt = ps->cnt;
+        l.base = ps->base;
+        l.E = ps->E;
+        l.id = ps->id;
+        l.queue = ps->queue;
+        l.out_macro = out.macro;
+        l.out_idx = out.max_idx;
+        l.verif = ctx->s.verification;
+        l.err = ctx->s.error;
+        XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
+                                          ctx->sm_count * ctx->batched_blocks_per_sm, l));
+        if (launches) *launches += 2;
+    }
     return XS_OK;
 }
 
@@ -240,11 +310,64 @@ static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int ch
     else
         k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
     XS_CUDA(cudaGetLastError());
-    const int lookup_blocks = ctx->sm_count * ctx->batched_blocks_per_sm;
-    XS_CUDA(batched_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, lookup_blocks, seg, cnt, sE,
-                                         sid, ctx->s.queue, out.macro, out.max_idx,
-                                         ctx->s.verification, ctx->s.error));
+    ListArgs l;
+    l.seg_v = seg;
+    l.cnt = cnt;
+    l.base = nullptr;
+    l.E = sE;
+    l.id = sid;
+    l.queue = ctx->s.queue;
+    l.out_macro = out.macro;
+    l.out_idx = out.max_idx;
+    l.verif = ctx->s.verification;
+    l.err = ctx->s.error;
+    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
+                                      ctx->sm_count * ctx->batched_blocks_per_sm, l));
     if (launches) *launches += 4;
+    return XS_OK;
+}
+
+// The (material, energy-bucket) counting sort alone, for the adjoint: fills
+// starts (bucket starts, before the scatter), offs (bucket ends, after it),
+// seg/cnt (padded material segments), sE and sid.
+xs_status enqueue_sort_only(xs_ctx *ctx, cudaStream_t st, long first, long count, int nb_log2,
+                            const SampleInput &in, int *offs, int *starts, int *seg, int *cnt,
+                            double *sE, int *sid)
+{
+    const int nb = 1 << nb_log2;
+    XS_CUDA(cudaMemsetAsync(offs, 0, (size_t)kMaterials * nb * 4, st));
+    const bool samples = in.energy != nullptr;
+    unsigned blocks;
+    if (samples) {
+        long want = (count + kBlock - 1) / kBlock;
+        long cap = (long)ctx->sm_count * 8;
+        blocks = (unsigned)(want < cap ? want : cap);
+        if (blocks == 0) blocks = 1;
+        k_sort_pass<true, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+    } else {
+        blocks = (unsigned)((count + (long)kBlock * kSortLpt - 1) / ((long)kBlock * kSortLpt));
+        k_sort_pass<false, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+    }
+    XS_CUDA(cudaGetLastError());
+    k_sort_scan<<<1, kScanThreads, 0, st>>>(offs, nb_log2, seg, cnt);
+    XS_CUDA(cudaGetLastError());
+    XS_CUDA(cudaMemcpyAsync(starts, offs, (size_t)kMaterials * nb * 4, cudaMemcpyDeviceToDevice, st));
+    if (samples)
+        k_sort_pass<true, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+    else
+        k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+    XS_CUDA(cudaGetLastError());
+    return XS_OK;
+}
+
+xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l, const double *sg,
+                                double *d_energy)
+{
+    typedef cudaError_t (*AdjFn)(const Tables &, cudaStream_t, int, const ListArgs &,
+                                 const double *, double *);
+    const int g = ctx->t.grid_type;
+    AdjFn f = g == XS_UNIONIZED ? unionized_adjoint : g == XS_NUCLIDE ? nuclide_adjoint : hash_adjoint;
+    XS_CUDA(f(ctx->t, st, ctx->sm_count * ctx->batched_blocks_per_sm, l, sg, d_energy));
     return XS_OK;
 }
 
@@ -264,9 +387,19 @@ xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first
     k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr,
                                                          nullptr, b.offs, b.sE, b.sid, b.error);
     XS_CUDA(cudaGetLastError());
-    XS_CUDA(batched_fn(ctx->t.grid_type)(ctx->t, st, arith, 0, ctx->sm_count * ctx->batched_blocks_per_sm,
-                                         b.seg, b.cnt, b.sE, b.sid, b.queue, out.macro,
-                                         out.max_idx, b.verification, b.error));
+    ListArgs l;
+    l.seg_v = b.seg;
+    l.cnt = b.cnt;
+    l.base = nullptr;
+    l.E = b.sE;
+    l.id = b.sid;
+    l.queue = b.queue;
+    l.out_macro = out.macro;
+    l.out_idx = out.max_idx;
+    l.verif = b.verification;
+    l.err = b.error;
+    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, 0,
+                                      ctx->sm_count * ctx->batched_blocks_per_sm, l));
     return XS_OK;
 }
 

@@ -9,6 +9,45 @@ namespace xsgb {
 
 constexpr int kBlock = 256;          // threads per block of every lookup kernel
 constexpr int kWarps = kBlock / 32;
+#ifndef XSGB_PLAIN_MIN_BLOCKS
+#define XSGB_PLAIN_MIN_BLOCKS 4      // resident blocks per SM the compiler must allow
+#endif
+
+// Arguments of the plain (tiled) lookup kernel.
+struct PlainArgs {
+    long first, count;
+    int tile;
+    const double *in_E;          // caller samples, or null: in-kernel LCG sampling
+    const int *in_mat;
+    double *out_macro;           // count*5 or null
+    unsigned char *out_idx;      // count or null
+    unsigned long long *verif;
+    int *err;
+    // overflow queues: each block runs only whole 32-lookup chunks and appends
+    // the rest of each material (< 32 lookups) here; null: run them padded
+    int *ovf_cnt;                // [12]
+    double *ovf_E;               // [12 * ovf_cap]
+    int *ovf_id;                 // [12 * ovf_cap]
+    int ovf_cap;                 // entries per material
+};
+
+// A material-segmented list of lookups (the batched sort, or the plain
+// kernel's overflow).  Chunk c covers virtual positions [32c, 32c+32); the
+// chunk's material m satisfies seg_v[m] <= 32c < seg_v[m+1] (each seg_v a
+// multiple of 32); entry p_v of material m sits at base[m] + (p_v - seg_v[m])
+// (base null: at p_v) and exists when p_v < seg_v[m] + cnt[m].
+struct ListArgs {
+    const int *seg_v;            // [13]
+    const int *cnt;              // [12]
+    const int *base;             // [12] or null
+    const double *E;
+    const int *id;
+    unsigned int *queue;
+    double *out_macro;
+    unsigned char *out_idx;
+    unsigned long long *verif;
+    int *err;
+};
 
 // Adds the per-lane verification counts of a block into *verif (one atomic).
 __device__ __forceinline__ void block_verification(unsigned long long mine,
@@ -44,29 +83,45 @@ __device__ __forceinline__ bool sample_at(const Tables &t, const double *in_E, c
     }
 }
 
+// One lookup of the event batch: macro_xs, argmax, outputs.
+template <int GRID, int ARITH, bool CHECKED>
+__device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, int m, long o,
+                                                     double *out_macro, unsigned char *out_idx,
+                                                     int *err)
+{
+    double macro[5];
+    macro_xs<GRID, ARITH, CHECKED>(t, E, m, macro, err);
+    const int arg = argmax5(macro);
+    if (out_macro) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
+    }
+    if (out_idx) out_idx[o] = (unsigned char)arg;
+    return (unsigned)(arg + 1);
+}
+
 // ---------------------------------------------------------------- PLAIN ---
 // One block = one tile of `tile` consecutive lookups.  The block samples them,
-// counting-sorts their ids by material in shared memory (each material's run
-// padded to a multiple of 32 so a warp never mixes materials), then its warps
-// pull 32-lookup chunks, fuel first, from a shared-memory queue and run one
-// lookup per lane.
+// counting-sorts their ids by material in shared memory, then its warps pull
+// 32-lookup chunks, fuel first, from a shared-memory queue and run one lookup
+// per lane, so a warp never mixes materials.  With overflow queues the last,
+// partial chunk of every material goes to the queue instead of running with
+// idle lanes.
 template <int GRID, int ARITH, bool CHECKED, bool SAMPLES>
-__global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long count, int tile,
-                                                  const double *in_E, const int *in_mat,
-                                                  double *out_macro, unsigned char *out_idx,
-                                                  unsigned long long *verif, int *err)
+__global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables t, PlainArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    const int tile = a.tile;
     double *sE = reinterpret_cast<double *>(smem);
     int *perm = reinterpret_cast<int *>(sE + tile);
     unsigned char *sMat = reinterpret_cast<unsigned char *>(perm + tile + kMaterials * 32);
-    __shared__ int cnt[kMaterials], cur[kMaterials], seg[kMaterials + 1];
+    __shared__ int cnt[kMaterials], cur[kMaterials], seg[kMaterials + 1], obase[kMaterials];
     __shared__ unsigned int qhead;
     __shared__ unsigned long long s_acc;
 
     const int tid = threadIdx.x;
     const long base = (long)blockIdx.x * tile;
-    const int ntile = (int)min((long)tile, count - base);
+    const int ntile = (int)min((long)tile, a.count - base);
     if (tid < kMaterials) cnt[tid] = 0;
     if (tid == 0) {
         qhead = 0;
@@ -82,7 +137,7 @@ __global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long cou
             unsigned long long seed = 0;
             double E;
             int m;
-            bool ok = sample_at<true>(t, in_E, in_mat, base + l, seed, E, m, err);
+            bool ok = sample_at<true>(t, a.in_E, a.in_mat, base + l, seed, E, m, a.err);
             sE[l] = E;
             sMat[l] = ok ? (unsigned char)m : 0xFF;
             if (ok) atomicAdd(&cnt[m], 1);
@@ -90,11 +145,12 @@ __global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long cou
     } else {
         const int l0 = tid * lpt;
         if (l0 < ntile) {
-            unsigned long long seed = lcg_skip(kStartingSeed, 2ULL * (unsigned long long)(first + base + l0));
+            unsigned long long seed =
+                lcg_skip(kStartingSeed, 2ULL * (unsigned long long)(a.first + base + l0));
             for (int q = 0; q < lpt && l0 + q < ntile; q++) {
                 double E;
                 int m;
-                sample_at<false>(t, nullptr, nullptr, 0, seed, E, m, err);
+                sample_at<false>(t, nullptr, nullptr, 0, seed, E, m, a.err);
                 sE[l0 + q] = E;
                 sMat[l0 + q] = (unsigned char)m;
                 atomicAdd(&cnt[m], 1);
@@ -102,6 +158,7 @@ __global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long cou
         }
     }
     __syncthreads();
+    const bool overflow = a.ovf_cnt != nullptr;
     if (tid == 0) {
         int s = 0;
         for (int m = 0; m < kMaterials; m++) {
@@ -111,12 +168,29 @@ __global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long cou
         }
         seg[kMaterials] = s;
     }
+    if (overflow && tid < kMaterials) {
+        const int rem = cnt[tid] & 31;
+        obase[tid] = rem ? atomicAdd(&a.ovf_cnt[tid], rem) : 0;
+    }
     __syncthreads();
     for (int l = tid; l < ntile; l += kBlock) {
         int m = sMat[l];
         if (m != 0xFF) perm[atomicAdd(&cur[m], 1)] = l;
     }
     __syncthreads();
+    if (overflow) {
+        // remainders: positions [seg+full, seg+cnt) of each material
+        for (int r = tid; r < kMaterials * 32; r += kBlock) {
+            const int m = r >> 5, q = r & 31;
+            const int full = cnt[m] & ~31;
+            if (q < (cnt[m] & 31)) {
+                const int l = perm[seg[m] + full + q];
+                const long slot = (long)m * a.ovf_cap + obase[m] + q;
+                a.ovf_E[slot] = sE[l];
+                a.ovf_id[slot] = (int)(base + l);
+            }
+        }
+    }
 
     unsigned long long mine = 0;
     const int lane = tid & 31;
@@ -129,41 +203,31 @@ __global__ void __launch_bounds__(kBlock) k_plain(Tables t, long first, long cou
         const int p = (int)c * 32 + lane;
         int m = 0;
         while (seg[m + 1] <= (int)c * 32) m++;
-        if (p < seg[m] + cnt[m]) {
+        const int limit = seg[m] + (overflow ? (cnt[m] & ~31) : cnt[m]);
+        if (p < limit) {
             const int l = perm[p];
-            const double E = sE[l];
-            double macro[5];
-            macro_xs<GRID, ARITH, CHECKED>(t, E, m, macro, err);
-            const int arg = argmax5(macro);
-            mine += (unsigned long long)(arg + 1);
-            const long o = base + l;
-            if (out_macro) {
-#pragma unroll
-                for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
-            }
-            if (out_idx) out_idx[o] = (unsigned char)arg;
+            mine += lookup_and_store<GRID, ARITH, CHECKED>(t, sE[l], m, base + l, a.out_macro,
+                                                           a.out_idx, a.err);
         }
     }
-    block_verification(mine, &s_acc, verif);
+    block_verification(mine, &s_acc, a.verif);
 }
 
-// -------------------------------------------------------------- BATCHED ---
-// Persistent lookup over the (material, energy-bucket)-sorted list.  Warps pull
-// 32-entry chunks from a global queue; the sorted order puts the fuel
-// material first, so the longest chunks start first.
+// ------------------------------------------------------ segmented lists ---
+// Persistent lookup over a material-segmented list (ListArgs).  Warps pull
+// 32-entry chunks from a global queue; fuel (material 0) comes first, so the
+// longest chunks start first.  No waits: a warp reads the queue once per chunk.
 template <int GRID, int ARITH, bool CHECKED>
-__global__ void __launch_bounds__(kBlock) k_batched_lookup(Tables t, const int *seg_g,
-                                                           const int *cnt_g, const double *sE,
-                                                           const int *sid, unsigned int *queue,
-                                                           double *out_macro,
-                                                           unsigned char *out_idx,
-                                                           unsigned long long *verif, int *err)
+__global__ void __launch_bounds__(kBlock) k_list_lookup(Tables t, ListArgs a)
 {
-    __shared__ int seg[kMaterials + 1], cnt[kMaterials];
+    __shared__ int seg[kMaterials + 1], cnt[kMaterials], bas[kMaterials];
     __shared__ unsigned long long s_acc;
     const int tid = threadIdx.x;
-    if (tid <= kMaterials) seg[tid] = seg_g[tid];
-    if (tid < kMaterials) cnt[tid] = cnt_g[tid];
+    if (tid <= kMaterials) seg[tid] = a.seg_v[tid];
+    if (tid < kMaterials) {
+        cnt[tid] = a.cnt[tid];
+        bas[tid] = a.base ? a.base[tid] : a.seg_v[tid];
+    }
     if (tid == 0) s_acc = 0;
     __syncthreads();
     const int nchunks = seg[kMaterials] >> 5;
@@ -171,27 +235,67 @@ __global__ void __launch_bounds__(kBlock) k_batched_lookup(Tables t, const int *
     unsigned long long mine = 0;
     for (;;) {
         unsigned int c = 0;
-        if (lane == 0) c = atomicAdd(queue, 1u);
+        if (lane == 0) c = atomicAdd(a.queue, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if ((int)c >= nchunks) break;
+        const int pv = (int)c * 32 + lane;
+        int m = 0;
+        while (seg[m + 1] <= (int)c * 32) m++;
+        if (pv < seg[m] + cnt[m]) {
+            const long p = (long)bas[m] + (pv - seg[m]);
+            mine += lookup_and_store<GRID, ARITH, CHECKED>(t, a.E[p], m, a.id[p], a.out_macro,
+                                                           a.out_idx, a.err);
+        }
+    }
+    block_verification(mine, &s_acc, a.verif);
+}
+
+// ------------------------------------------------------- adjoint, energy ---
+// Over the adjoint's sorted list: the forward macro_xs (FAST arithmetic) and
+// dL/dE = sum_c gbar_c * sum_j conc_j * slope_jc, per lookup.  sg holds the
+// upstream gradients in sorted order (5 per position).
+template <int GRID>
+__global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, const double *sg,
+                                                         double *d_energy)
+{
+    __shared__ int seg[kMaterials + 1], cnt[kMaterials];
+    __shared__ unsigned long long s_acc;
+    const int tid = threadIdx.x;
+    if (tid <= kMaterials) seg[tid] = a.seg_v[tid];
+    if (tid < kMaterials) cnt[tid] = a.cnt[tid];
+    if (tid == 0) s_acc = 0;
+    __syncthreads();
+    const int nchunks = seg[kMaterials] >> 5;
+    const int lane = tid & 31;
+    unsigned long long mine = 0;
+    for (;;) {
+        unsigned int c = 0;
+        if (lane == 0) c = atomicAdd(a.queue, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
         if ((int)c >= nchunks) break;
         const int p = (int)c * 32 + lane;
         int m = 0;
         while (seg[m + 1] <= (int)c * 32) m++;
         if (p < seg[m] + cnt[m]) {
-            const double E = sE[p];
-            const int id = sid[p];
-            double macro[5];
-            macro_xs<GRID, ARITH, CHECKED>(t, E, m, macro, err);
+            const long id = a.id[p];
+            double macro[5], S[5];
+            macro_xs<GRID, XS_ARITH_FAST, false, true>(t, a.E[p], m, macro, a.err, S);
             const int arg = argmax5(macro);
-            mine += (unsigned long long)(arg + 1);
-            if (out_macro) {
+            mine += (unsigned)(arg + 1);
+            if (a.out_macro) {
 #pragma unroll
-                for (int k = 0; k < 5; k++) out_macro[(long)id * 5 + k] = macro[k];
+                for (int k = 0; k < 5; k++) a.out_macro[id * 5 + k] = macro[k];
             }
-            if (out_idx) out_idx[id] = (unsigned char)arg;
+            if (d_energy) {
+                const double *g = sg + (long)p * 5;
+                double dE = 0.0;
+#pragma unroll
+                for (int k = 0; k < 5; k++) dE = fma(g[k], S[k], dE);
+                d_energy[id] = dE;
+            }
         }
     }
-    block_verification(mine, &s_acc, verif);
+    block_verification(mine, &s_acc, a.verif);
 }
 
 // -------------------------------------------------------------- HISTORY ---
@@ -229,24 +333,28 @@ __global__ void __launch_bounds__(kBlock) k_history(Tables t, long first, long c
 }
 
 // ------------------------------------------------------------ launchers ---
+inline size_t plain_smem_bytes(int tile)
+{
+    return (size_t)tile * 8 + (size_t)(tile + kMaterials * 32) * 4 + tile;
+}
+
 template <int GRID>
 struct GridLaunch {
     static cudaError_t plain(const Tables &t, cudaStream_t st, int arith, int checked,
-                             bool samples, long first, long count, int tile, const double *in_E,
-                             const int *in_mat, double *out_macro, unsigned char *out_idx,
-                             unsigned long long *verif, int *err)
+                             bool samples, const PlainArgs &a)
     {
-        const long blocks = (count + tile - 1) / tile;
-        const size_t sm = (size_t)tile * 8 + (size_t)(tile + kMaterials * 32) * 4 + tile;
-#define XSGB_PLAIN(A, C, S)                                                               \
-    do {                                                                                  \
-        auto k = k_plain<GRID, A, C, S>;                                                  \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                             (int)sm);                                    \
-        if (e != cudaSuccess) return e;                                                   \
-        k<<<(unsigned)blocks, kBlock, sm, st>>>(t, first, count, tile, in_E, in_mat,      \
-                                                out_macro, out_idx, verif, err);          \
-        return cudaGetLastError();                                                        \
+        const long blocks = (a.count + a.tile - 1) / a.tile;
+        const size_t sm = plain_smem_bytes(a.tile);
+#define XSGB_PLAIN(A, C, S)                                                                   \
+    do {                                                                                      \
+        auto k = k_plain<GRID, A, C, S>;                                                      \
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                             (int)sm);                                        \
+        if (e == cudaSuccess)                                                                 \
+            e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 25);  \
+        if (e != cudaSuccess) return e;                                                       \
+        k<<<(unsigned)blocks, kBlock, sm, st>>>(t, a);                                        \
+        return cudaGetLastError();                                                            \
     } while (0)
         if (checked) {
             if (samples) XSGB_PLAIN(XS_ARITH_FAST, true, true);
@@ -261,22 +369,18 @@ struct GridLaunch {
 #undef XSGB_PLAIN
     }
 
-    static cudaError_t batched(const Tables &t, cudaStream_t st, int arith, int checked,
-                               int blocks, const int *seg, const int *cnt, const double *sE,
-                               const int *sid, unsigned int *queue, double *out_macro,
-                               unsigned char *out_idx, unsigned long long *verif, int *err)
+    static cudaError_t list(const Tables &t, cudaStream_t st, int arith, int checked, int blocks,
+                            const ListArgs &a)
     {
-#define XSGB_BATCHED(A, C)                                                                    \
-    do {                                                                                      \
-        k_batched_lookup<GRID, A, C><<<blocks, kBlock, 0, st>>>(t, seg, cnt, sE, sid, queue,  \
-                                                                out_macro, out_idx, verif,    \
-                                                                err);                         \
-        return cudaGetLastError();                                                            \
+#define XSGB_LIST(A, C)                                                      \
+    do {                                                                     \
+        k_list_lookup<GRID, A, C><<<blocks, kBlock, 0, st>>>(t, a);          \
+        return cudaGetLastError();                                           \
     } while (0)
-        if (checked) XSGB_BATCHED(XS_ARITH_FAST, true);
-        if (arith == XS_ARITH_EXACT) XSGB_BATCHED(XS_ARITH_EXACT, false);
-        XSGB_BATCHED(XS_ARITH_FAST, false);
-#undef XSGB_BATCHED
+        if (checked) XSGB_LIST(XS_ARITH_FAST, true);
+        if (arith == XS_ARITH_EXACT) XSGB_LIST(XS_ARITH_EXACT, false);
+        XSGB_LIST(XS_ARITH_FAST, false);
+#undef XSGB_LIST
     }
 
     static cudaError_t history(const Tables &t, cudaStream_t st, int arith, long first,
@@ -294,40 +398,38 @@ struct GridLaunch {
 // Per-grid entry points (defined in lookup_<grid>.cu).
 #define XSGB_DECLARE_GRID(NAME)                                                               \
     cudaError_t NAME##_plain(const Tables &t, cudaStream_t st, int arith, int checked,          \
-                             bool samples, long first, long count, int tile, const double *in_E, \
-                             const int *in_mat, double *out_macro, unsigned char *out_idx,       \
-                             unsigned long long *verif, int *err);                               \
-    cudaError_t NAME##_batched(const Tables &t, cudaStream_t st, int arith, int checked,        \
-                               int blocks, const int *seg, const int *cnt, const double *sE,     \
-                               const int *sid, unsigned int *queue, double *out_macro,           \
-                               unsigned char *out_idx, unsigned long long *verif, int *err);     \
+                             bool samples, const PlainArgs &a);                                 \
+    cudaError_t NAME##_list(const Tables &t, cudaStream_t st, int arith, int checked,           \
+                            int blocks, const ListArgs &a);                                     \
     cudaError_t NAME##_history(const Tables &t, cudaStream_t st, int arith, long first,         \
-                               long count, int nl, unsigned long long *verif, int *err);
+                               long count, int nl, unsigned long long *verif, int *err);        \
+    cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
+                               const double *sg, double *d_energy);
 XSGB_DECLARE_GRID(unionized)
 XSGB_DECLARE_GRID(nuclide)
 XSGB_DECLARE_GRID(hash)
 
 #define XSGB_DEFINE_GRID(NAME, GRID)                                                            \
     cudaError_t NAME##_plain(const Tables &t, cudaStream_t st, int arith, int checked,          \
-                             bool samples, long first, long count, int tile, const double *in_E, \
-                             const int *in_mat, double *out_macro, unsigned char *out_idx,       \
-                             unsigned long long *verif, int *err)                                \
+                             bool samples, const PlainArgs &a)                                  \
     {                                                                                           \
-        return GridLaunch<GRID>::plain(t, st, arith, checked, samples, first, count, tile, in_E, \
-                                       in_mat, out_macro, out_idx, verif, err);                  \
+        return GridLaunch<GRID>::plain(t, st, arith, checked, samples, a);                      \
     }                                                                                           \
-    cudaError_t NAME##_batched(const Tables &t, cudaStream_t st, int arith, int checked,        \
-                               int blocks, const int *seg, const int *cnt, const double *sE,     \
-                               const int *sid, unsigned int *queue, double *out_macro,           \
-                               unsigned char *out_idx, unsigned long long *verif, int *err)      \
+    cudaError_t NAME##_list(const Tables &t, cudaStream_t st, int arith, int checked,           \
+                            int blocks, const ListArgs &a)                                      \
     {                                                                                           \
-        return GridLaunch<GRID>::batched(t, st, arith, checked, blocks, seg, cnt, sE, sid, queue, \
-                                         out_macro, out_idx, verif, err);                        \
+        return GridLaunch<GRID>::list(t, st, arith, checked, blocks, a);                        \
     }                                                                                           \
     cudaError_t NAME##_history(const Tables &t, cudaStream_t st, int arith, long first,         \
                                long count, int nl, unsigned long long *verif, int *err)          \
     {                                                                                           \
         return GridLaunch<GRID>::history(t, st, arith, first, count, nl, verif, err);           \
+    }                                                                                           \
+    cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
+                               const double *sg, double *d_energy)                              \
+    {                                                                                           \
+        k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, sg, d_energy);                    \
+        return cudaGetLastError();                                                              \
     }
 
 }  // namespace xsgb

@@ -114,7 +114,7 @@ xs_status build_derived_tables(xs_ctx *ctx)
     k_records<<<grid_for(t.n_iso * (t.n_gp - 1), sm), 256, 0, st>>>(t.grid, t.n_iso, t.n_gp, (double2 *)p);
     XS_CUDA(cudaGetLastError());
 
-    if (t.grid_type != XS_UNIONIZED) {
+    {   // every grid type: the searches of the hash / nuclide grids and the adjoint
         s = ctx_alloc(ctx, &p, (size_t)n_points * 8);
         if (s != XS_OK) return s;
         t.ekeys = (const long long *)p;

@@ -44,6 +44,11 @@ struct Tables {
     const int *union_bins;           // [2^b + 1]
     const int *index_grid;           // UEG: [n_union * n_iso]  HASH: [hash_bins * n_iso]
     double mat_thresh[kMaterials];   // pick_mat running sums, Simulation.c:450-457
+    int mat_lo[kMaterials];          // smallest / largest nuclide id of each material
+    int mat_hi[kMaterials];          //   (span of the index-row prefetch)
+    int pair_base[kMaterials + 1];   // running sum of num_nucs: (material, position) pairs
+    const int *inv_off;              // [n_iso + 1] pairs holding each nuclide (CSR)
+    const int *inv_pair;             // [pairs] m * max_nucs + j, by nuclide, m ascending
 };
 
 // Per-run scratch in device memory (owned by the context).
@@ -55,6 +60,10 @@ struct Scratch {
     size_t sort_bytes = 0;
     void *stage = nullptr;                       // staging for host outputs
     size_t stage_bytes = 0;
+    void *plain_buf = nullptr;                   // plain-kernel overflow queues
+    size_t plain_bytes = 0;
+    void *adj_buf = nullptr;                     // adjoint sort, tables and partials
+    size_t adj_bytes = 0;
 };
 
 struct BatchedGraph {
@@ -116,9 +125,22 @@ struct SampleInput {
     const double *energy = nullptr;   // device, or null: in-kernel LCG sampling
     const int *mat = nullptr;
 };
+// Overflow queues of the plain kernel (see PlainArgs in lookup_kernels.cuh).
+struct PlainScratch {
+    int *cnt;            // [12] entries per material
+    int *seg_v;          // [13] packed chunk starts
+    int *base;           // [12] m * cap
+    unsigned int *queue;
+    double *E;           // [12 * cap]
+    int *id;             // [12 * cap]
+    int cap;
+};
+size_t plain_scratch_bytes(long count, int tile);
+PlainScratch carve_plain_scratch(void *buf, long count, int tile);
+// ps == null: each block runs the partial chunks of its tile with idle lanes.
 xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                       long count, int block, int tile, const SampleInput &in,
-                       const Outputs &out, int *launches);
+                       long count, int tile, const SampleInput &in, const Outputs &out,
+                       const PlainScratch *ps, int *launches);
 xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                          long count, int block, int buckets, const SampleInput &in,
                          const Outputs &out, int *launches);
@@ -139,6 +161,17 @@ struct BatchedScratch {
 xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
                              int nb_log2, const BatchedScratch &b, const Outputs &out);
 xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat);
+
+struct ListArgs;
+xs_status enqueue_sort_only(xs_ctx *ctx, cudaStream_t st, long first, long count, int nb_log2,
+                            const SampleInput &in, int *offs, int *starts, int *seg, int *cnt,
+                            double *sE, int *sid);
+xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l, const double *sg,
+                                double *d_energy);
+// adjoint.cu: the whole adjoint on `st` (all pointers device memory)
+xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
+                         const SampleInput &in, const double *gbar, double *macro_out,
+                         double *d_concs, double *d_xs, double *d_energy, int *launches);
 
 // host setup (setup_host.cu)
 void pick_mat_thresholds(double out[kMaterials]);
