@@ -249,6 +249,8 @@ def main():
                     help="override gridpoints per nuclide (a smaller case of the workload, for profiling)")
     ap.add_argument("--buckets", type=int, default=0, help="batched: energy buckets per material")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="also time forward+adjoint (xs_run_adjoint, device arrays) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     args = ap.parse_args()
@@ -336,6 +338,31 @@ def main():
     e2e_ok = re.verification == last.verification
     e2e_value = world * N / statistics.median(e2e_t)
 
+    adj = None
+    if args.adjoint:
+        g = torch.randn((N, 5), dtype=torch.float64, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(1234))
+        d_e = torch.empty(N, dtype=torch.float64, device="cuda")
+        d_c = torch.zeros((12, problem.sd.max_num_nucs), dtype=torch.float64, device="cuda")
+        d_x = torch.zeros((inputs.n_isotopes, inputs.n_gridpoints, 5), dtype=torch.float64,
+                          device="cuda")
+        macro = torch.empty((N, 5), dtype=torch.float64, device="cuda")
+        akw = dict(first=first, count=N, stream=stream, macro_out=macro, d_concs=d_c, d_xs=d_x,
+                   d_energy=d_e)
+        for _ in range(2):
+            ctx.adjoint(g, **akw)
+        times = []
+        launches_adj = 0
+        for _ in range(max(3, args.steps // 4)):
+            ra = ctx.adjoint(g, **akw)
+            times.append(ra.device_ms)
+            launches_adj = ra.kernel_launches
+        t_adj = statistics.median(times) / 1e3
+        adj = {"value": N / t_adj, "unit": UNIT, "ms_per_step": t_adj * 1e3,
+               "vs_forward": (N / t_adj) / (N * args.steps / t), "kernel_launches": launches_adj,
+               "hash_ok": ra.hash == last.hash,
+               "what": "forward macro_xs + dL/dE + dL/dconcs + dL/dxs, device arrays"}
+
     line = None
     if rank == 0:
         bpl = algorithmic_bytes_per_lookup(inputs, list(problem.arrays()["num_nucs"]))
@@ -369,6 +396,7 @@ def main():
                     "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",
                     "verification_matches": bool(e2e_ok)},
             "gpu_launches": launches,
+            "forward_adjoint": adj,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

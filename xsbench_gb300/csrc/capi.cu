@@ -689,7 +689,7 @@ static xs_status adjoint_common(xs_ctx *ctx, const xs_run_opts *opts, const doub
         // one staging block: samples, gbar, outputs, zeroed gradient sums
         const size_t bytes = (samples ? (size_t)n * 12 : 0) + (size_t)n * 40 +
                              (macro_out ? (size_t)n * 40 : 0) + (d_energy ? (size_t)n * 8 : 0) +
-                             (d_concs ? nconc * 8 : 0) + (d_xs ? nxs * 8 : 0) + 1024;
+                             (d_concs ? nconc * 8 : 0) + (d_xs ? nxs * 8 : 0) + 8 * 256;
         s = ensure_stage(ctx, bytes);
         if (s != XS_OK) return s;
         char *b = (char *)ctx->s.stage;
