@@ -279,7 +279,8 @@ def main():
     problem = X.grid_init(inputs)
     ctx = X.Context(inputs, problem, device=local)
     t_setup = time.perf_counter() - t_setup
-    first = rank * N
+    from xsbench_gb300.shard import reduce_time_max, shard_range
+    first, N = shard_range(rank, world, N, "weak")
     # a non-default stream: its handle goes to the library and the events
     # below are recorded on it
     stream = torch.cuda.Stream()
@@ -314,11 +315,7 @@ def main():
     if dist:
         dist.barrier()
     t = ev0.elapsed_time(ev1) / 1e3
-    t_max = t
-    if dist:
-        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = reduce_time_max(t, dist)
     value = world * N * args.steps / t_max
     hash_ok = hash_ok and (rank != 0 or expected is None or N != 17000000
                            or last.hash == expected)

@@ -233,10 +233,20 @@ xs_status xs_adjoint_samples(xs_ctx *ctx, const xs_run_opts *opts, const double 
                              double *d_concs, double *d_xs, double *d_energy,
                              xs_run_result *result);
 
-/* Times the kernel shapes on this context and keeps the fastest as its
- * defaults; with cache_path non-NULL the choice is read from / merged into a
- * JSON cache keyed by (device name, problem). */
+/* Autotuner (no reference counterpart).  Times, on a sample of up to 4M of
+ * the context's event lookups, the plain kernel's tile sizes, the batched
+ * kernel's energy buckets, the persistent kernels' blocks per SM and every
+ * grid type the context can serve (it derives a 10,000-bin hash grid and the
+ * nuclide grid's search keys on the device when missing; all grid types give
+ * the same intervals), installs the fastest as the context's defaults and
+ * returns it in *best (kernel, tile_lookups, energy_buckets).  With
+ * cache_path non-NULL the choice is read from, or merged into, a JSON file
+ * keyed by (device name, problem), and a cached choice is installed without
+ * timing. */
 xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best);
+
+/* Grid type the context currently looks up with (changes after xs_autotune). */
+int xs_ctx_grid_type(const xs_ctx *ctx);
 
 /* Allocation-free batched run.  It has no counterpart in the reference.
  * The same lookups as xs_run_event with the BATCHED kernel, for callers that

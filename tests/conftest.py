@@ -30,6 +30,8 @@ CONFIGS = {
     "large_unionized": dict(size="large", grid="unionized"),
     "large_hash": dict(size="large", grid="hash"),
     "large_nuclide": dict(size="large", grid="nuclide"),
+    "xl_hash": dict(size="XL", grid="hash", lookups=100000000),
+    "xl_nuclide": dict(size="XL", grid="nuclide", lookups=100000000),
 }
 
 

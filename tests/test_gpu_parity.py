@@ -100,6 +100,27 @@ def test_full_size_against_reference(name):
     assert r.verification == g["verification"]
 
 
+@pytest.mark.parametrize("name", ["xl_hash", "xl_nuclide"])
+def test_xl_against_reference(name):
+    """XL (355 x 238,847 points, 100M lookups).  The reference has no XL
+    constant (io.c:85-106); the digests come from its own build.  The nuclide
+    grid gives the same interval as the hash grid for every lookup, so both
+    are held to the hash-grid digests."""
+    g = golden_json("full_xl_hash")
+    gl = golden_npz("lookups_xl_hash")
+    ctx = ctx_for(name)
+    n = g["lookups"]
+    r, m, i = run(ctx, n, kernel="batched", arith="exact")
+    assert r.verification == g["verification"] and r.hash == 156835
+    assert sha(i) == g["sha256_max_idx"]
+    assert sha(m) == g["sha256_macro_xs"]
+    assert np.array_equal(m[gl["index"]], gl["macro_xs"])
+    del m
+    for kernel in ("plain", "batched"):
+        r = ctx.run_event(kernel=kernel, arith="fast")
+        assert r.verification == g["verification"], kernel
+
+
 def test_verification_only_runs_match():
     g = golden_json("full_tiny_hash")
     ctx = ctx_for("tiny_hash")

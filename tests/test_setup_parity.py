@@ -15,7 +15,7 @@ from conftest import golden_json, oracle_config, product_inputs, sha
 
 @pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "tiny_nuclide",
                                   "small_unionized", "small_hash", "small_nuclide",
-                                  "large_hash", "large_nuclide", "large_unionized"])
+                                  "large_hash", "large_nuclide", "large_unionized", "xl_hash"])
 def test_grid_init_matches_reference(name):
     g = golden_json("setup_" + name)
     with X.grid_init(product_inputs(name)) as p:

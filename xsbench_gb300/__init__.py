@@ -104,6 +104,7 @@ _SIGNATURES = {
     "xs_adjoint_samples": ([C.c_void_p, _P(RunOpts), C.c_void_p, C.c_void_p, C.c_long, C.c_void_p,
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _P(RunResult)], C.c_int),
     "xs_autotune": ([C.c_void_p, C.c_char_p, _P(RunOpts)], C.c_int),
+    "xs_ctx_grid_type": ([C.c_void_p], C.c_int),
     "xs_run_event_based_simulation": ([Inputs, SimData, C.c_int, _P(C.c_ulonglong)], C.c_int),
     "xs_run_event_batched_static": ([C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int, C.c_void_p,
                                      C.c_void_p, C.c_void_p, _P(C.c_ulonglong)], C.c_int),
@@ -361,6 +362,18 @@ class Context:
             _check(lib().xs_adjoint_samples(self._h, C.byref(o), pe, pm, n, *a, C.byref(r)),
                    "xs_adjoint_samples")
         return Result(r)
+
+    def autotune(self, cache_path: str | None = None) -> dict:
+        """Time the kernel shapes and grid types and keep the fastest (xs_autotune)."""
+        o = RunOpts()
+        _check(lib().xs_autotune(self._h, cache_path.encode() if cache_path else None,
+                                 C.byref(o)), "xs_autotune")
+        return {"kernel": ("plain", "batched")[o.kernel], "tile": o.tile_lookups,
+                "buckets": o.energy_buckets, "grid": self.grid_type}
+
+    @property
+    def grid_type(self) -> str:
+        return {0: "unionized", 1: "nuclide", 2: "hash"}[lib().xs_ctx_grid_type(self._h)]
 
     def sync(self) -> Result:
         r = RunResult()

@@ -127,6 +127,74 @@ __global__ void k_gather_gbar(const int *seg, const int *cnt, const int *sid, co
     }
 }
 
+// ------------------------------------------------------- prefix of gbar ---
+// EP[p] = sum_{q < p} sg[q] per channel, over all P positions (padding holds
+// zeros), by a three-phase scan with a fixed shape: block sums, one-block scan
+// of the block sums, block-local scan plus offset.
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(const int *seg, const double *sg,
+                                                            double *bsum)
+{
+    __shared__ double red[kScanBlock];
+    const int total = seg[kMaterials];
+    const int nblocks = (total + kScanBlock - 1) / kScanBlock;
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        for (int c = 0; c < 5; c++) {
+            const long p = (long)b * kScanBlock + threadIdx.x;
+            red[threadIdx.x] = p < total ? sg[p * 5 + c] : 0.0;
+            __syncthreads();
+            for (int w = kScanBlock / 2; w > 0; w >>= 1) {
+                if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) bsum[(long)b * 5 + c] = red[0];
+            __syncthreads();
+        }
+    }
+}
+
+// exclusive scan of the block sums, sequentially in block order (one thread
+// per channel)
+__global__ void k_scan_bsums(const int *seg, double *bsum)
+{
+    const int c = threadIdx.x;
+    if (c >= 5) return;
+    const int nblocks = (seg[kMaterials] + kScanBlock - 1) / kScanBlock;
+    double run = 0.0;
+    for (int b = 0; b < nblocks; b++) {
+        const double v = bsum[(long)b * 5 + c];
+        bsum[(long)b * 5 + c] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_local(const int *seg, const double *sg,
+                                                           const double *bsum, double *ep)
+{
+    __shared__ double buf[kScanBlock];
+    const int total = seg[kMaterials];
+    const int nblocks = (total + kScanBlock - 1) / kScanBlock;
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        for (int c = 0; c < 5; c++) {
+            const long p = (long)b * kScanBlock + threadIdx.x;
+            buf[threadIdx.x] = p < total ? sg[p * 5 + c] : 0.0;
+            __syncthreads();
+            // Hillis-Steele inclusive scan (fixed shape)
+            for (int o = 1; o < kScanBlock; o <<= 1) {
+                const double v = threadIdx.x >= o ? buf[threadIdx.x - o] : 0.0;
+                __syncthreads();
+                buf[threadIdx.x] += v;
+                __syncthreads();
+            }
+            const double excl = (threadIdx.x ? buf[threadIdx.x - 1] : 0.0);
+            if (p < total) ep[p * 5 + c] = bsum[(long)b * 5 + c] + excl;
+            if (p == total - 1) ep[(long)total * 5 + c] = bsum[(long)b * 5 + c] + buf[threadIdx.x];
+            __syncthreads();
+        }
+    }
+}
+
 // ---------------------------------------------------- transposed layout ---
 struct AdjLayout {
     int nchunks[kMaterials];
@@ -169,8 +237,9 @@ __device__ __forceinline__ void store10(double *dst, const double A[5], const do
 // The transposed pass (see the file comment, step 4).
 __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg, const int *cnt,
                                                         const double *sE, const double *sg,
-                                                        const AdjLayout *L, unsigned int *queue,
-                                                        double *table, double *slots)
+                                                        const double *ep, const AdjLayout *L,
+                                                        unsigned int *queue, double *table,
+                                                        double *slots)
 {
     __shared__ AdjLayout lay;
     __shared__ int s_seg[kMaterials + 1], s_cnt[kMaterials];
@@ -219,11 +288,16 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
         const long k_first = k;
         long long next_key = (k + 1 <= t.n_gp - 2) ? ek[k + 1] : 0x7FFFFFFFFFFFFFFFLL;
         double e_hi = t.grid[(long)nuc * t.n_gp + k + 1].energy;
-        double A[5] = {0, 0, 0, 0, 0}, Gs[5] = {0, 0, 0, 0, 0};
+        double A[5] = {0, 0, 0, 0, 0}, Gs[5];
+        long i_start = a;   // first position of the current interval in this chunk
         for (long i = a; i < b; i++) {
             const double E = sE[i];
             const long long q = order_key(E);
             if (q >= next_key) {
+                // G over [i_start, i) from the prefix of gbar
+#pragma unroll
+                for (int cc = 0; cc < 5; cc++) Gs[cc] = ep[i * 5 + cc] - ep[i_start * 5 + cc];
+                i_start = i;
                 // leave interval k: the first one goes to slot 0, later ones into the table
                 if (k == k_first) {
                     slot[0] = __longlong_as_double(k);
@@ -237,16 +311,15 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
                 } while (q >= next_key);
                 e_hi = t.grid[(long)nuc * t.n_gp + k + 1].energy;
 #pragma unroll
-                for (int cc = 0; cc < 5; cc++) A[cc] = Gs[cc] = 0.0;
+                for (int cc = 0; cc < 5; cc++) A[cc] = 0.0;
             }
             const double d = e_hi - E;
             const double *g = sg + i * 5;
 #pragma unroll
-            for (int cc = 0; cc < 5; cc++) {
-                A[cc] = fma(g[cc], d, A[cc]);
-                Gs[cc] += g[cc];
-            }
+            for (int cc = 0; cc < 5; cc++) A[cc] = fma(g[cc], d, A[cc]);
         }
+#pragma unroll
+        for (int cc = 0; cc < 5; cc++) Gs[cc] = ep[b * 5 + cc] - ep[i_start * 5 + cc];
         if (k == k_first) {
             slot[0] = __longlong_as_double(k);
             store10(slot + 1, A, Gs);
@@ -259,26 +332,50 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
     }
 }
 
-// Boundary slots into the table, chunk by chunk in order, one thread per pair.
+// Boundary slots into the table.  Interval k's boundary pieces sit in
+// consecutive chunks (the last interval of chunk c, the first of chunk c+1,
+// and onwards while a chunk holds k only).  The chunk holding the first piece
+// owns k and adds the pieces in chunk order, so the sum is deterministic;
+// owners work in parallel over (pair, chunk, side).
 __global__ void k_adj_fixup(Tables t, const AdjLayout *L, const double *slots, double *table)
 {
-    const int pair = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pair >= t.pair_base[kMaterials]) return;
-    int m = 0;
-    while (t.pair_base[m + 1] <= pair) m++;
-    const int j = pair - t.pair_base[m];
     const long n_int = t.n_gp - 1;
-    double *tab = table + (long)pair * n_int * kTbl;
-    const int nch = L->nchunks[m];
-    for (int c = 0; c < nch; c++) {
-        const double *sl = slots + (L->slot_base[m] + ((long)j * nch + c) * 2) * kSlot;
-        for (int side = 0; side < 2; side++) {
-            const long k = __double_as_longlong(sl[side * kSlot]);
-            if (k < 0) continue;
-            double *dst = tab + k * kTbl;
-#pragma unroll
-            for (int v = 0; v < kTbl; v++) dst[v] += sl[side * kSlot + 1 + v];
+    long total = 0;
+    for (int m = 0; m < kMaterials; m++) total += (long)t.num_nucs[m] * L->nchunks[m] * 2;
+    for (long w = (long)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += (long)gridDim.x * blockDim.x) {
+        int m = 0;
+        while (m + 1 < kMaterials && L->slot_base[m + 1] <= w) m++;
+        const long local = w - L->slot_base[m];
+        const int nch = L->nchunks[m];
+        const int j = (int)(local / (2L * nch));
+        const int c = (int)((local / 2) % nch);
+        const int side = (int)(local & 1);
+        const double *base = slots + (L->slot_base[m] + (long)j * nch * 2) * kSlot;
+        const double *sl = base + ((long)c * 2 + side) * kSlot;
+        const long k = __double_as_longlong(sl[0]);
+        if (k < 0) continue;
+        if (side == 0 && c > 0) {
+            // a chain started earlier owns k if the previous piece holds it
+            const double *prev = base + ((long)(c - 1) * 2) * kSlot;
+            const long k1 = __double_as_longlong(prev[kSlot]);
+            const long kp = k1 >= 0 ? k1 : __double_as_longlong(prev[0]);
+            if (kp == k) continue;
         }
+        double acc[kTbl];
+#pragma unroll
+        for (int v = 0; v < kTbl; v++) acc[v] = sl[1 + v];
+        // later chunks: their first piece continues the chain while it holds k
+        for (int cc = c + 1; cc < nch; cc++) {
+            const double *nx = base + ((long)cc * 2) * kSlot;
+            if (__double_as_longlong(nx[0]) != k) break;
+#pragma unroll
+            for (int v = 0; v < kTbl; v++) acc[v] += nx[1 + v];
+            if (__double_as_longlong(nx[kSlot]) >= 0) break;  // the chunk moved past k
+        }
+        double *dst = table + ((long)(t.pair_base[m] + j) * n_int + k) * kTbl;
+#pragma unroll
+        for (int v = 0; v < kTbl; v++) dst[v] += acc[v];
     }
 }
 
@@ -377,6 +474,8 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     const size_t o_sE = off; off = align256(off + padded * 8);
     const size_t o_sid = off; off = align256(off + padded * 4);
     const size_t o_sg = off; off = align256(off + padded * 40);
+    const size_t o_ep = off; off = align256(off + (padded + 1) * 40);
+    const size_t o_bsum = off; off = align256(off + (padded / kScanBlock + 2) * 40);
     const size_t o_table = off; off = align256(off + (size_t)pairs * n_int * kTbl * 8);
     const size_t o_slots = off; off = align256(off + slot_count * kSlot * 8);
     const size_t need = off;
@@ -403,6 +502,8 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     double *sE = (double *)(B + o_sE);
     int *sid = (int *)(B + o_sid);
     double *sg = (double *)(B + o_sg);
+    double *ep = (double *)(B + o_ep);
+    double *bsum = (double *)(B + o_bsum);
     double *table = (double *)(B + o_table);
     double *slots = (double *)(B + o_slots);
 
@@ -437,11 +538,15 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
         XS_CUDA(cudaMemsetAsync(queue + 4, 0, 4, st));
         k_adj_layout<<<1, 32, 0, st>>>(t, cnt, L);
         XS_CUDA(cudaGetLastError());
-        k_adj_transposed<<<ctx->sm_count * 4, 256, 0, st>>>(t, seg, cnt, sE, sg, L, queue + 4, table, slots);
+        k_scan_blocks<<<ctx->sm_count * 2, kScanBlock, 0, st>>>(seg, sg, bsum);
+        k_scan_bsums<<<1, 32, 0, st>>>(seg, bsum);
+        k_scan_local<<<ctx->sm_count * 2, kScanBlock, 0, st>>>(seg, sg, bsum, ep);
         XS_CUDA(cudaGetLastError());
-        k_adj_fixup<<<(pairs + 127) / 128, 128, 0, st>>>(t, L, slots, table);
+        k_adj_transposed<<<ctx->sm_count * 4, 256, 0, st>>>(t, seg, cnt, sE, sg, ep, L, queue + 4, table, slots);
         XS_CUDA(cudaGetLastError());
-        n += 3;
+        k_adj_fixup<<<ctx->sm_count * 8, 256, 0, st>>>(t, L, slots, table);
+        XS_CUDA(cudaGetLastError());
+        n += 6;
         if (d_xs) {
             const long npts = (long)t.n_iso * t.n_gp;
             const long want = (npts + 255) / 256;

@@ -355,13 +355,17 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
         t.n_union = sd->length_unionized_energy_array;
         s = upload(ctx, sd->unionized_energy_array, (size_t)t.n_union, &t.union_e);
     }
-    if (s == XS_OK && in->grid_type != XS_NUCLIDE)
+    if (s == XS_OK && in->grid_type != XS_NUCLIDE) {
         s = upload(ctx, sd->index_grid, (size_t)sd->length_index_grid, &t.index_grid);
+        ctx->own_index = t.index_grid;
+    }
     if (s == XS_OK) s = build_derived_tables(ctx);
     if (s != XS_OK) {
         xs_ctx_destroy(ctx);
         return s;
     }
+    ctx->base_coarse = t.coarse;
+    ctx->base_n_coarse = t.n_coarse;
     *out = ctx;
     return XS_OK;
 }
@@ -391,17 +395,18 @@ xs_status xs_ctx_download(xs_ctx *ctx, xs_simdata *out)
     r.concs = (double *)malloc(sizeof(double) * (size_t)r.length_concs);
     r.nuclide_grid = (xs_gridpoint *)malloc(sizeof(xs_gridpoint) * (size_t)n_pts);
     long n_index = 0;
-    if (t.grid_type == XS_UNIONIZED) {
+    const int gtype = ctx->inputs.grid_type;
+    if (gtype == XS_UNIONIZED) {
         r.length_unionized_energy_array = (int)t.n_union;
         r.unionized_energy_array = (double *)malloc(sizeof(double) * (size_t)t.n_union);
         n_index = t.n_union * t.n_iso;
-    } else if (t.grid_type == XS_HASH) {
-        n_index = (long)t.hash_bins * t.n_iso;
+    } else if (gtype == XS_HASH) {
+        n_index = (long)ctx->inputs.hash_bins * t.n_iso;
     }
     r.length_index_grid = n_index;
     if (n_index) r.index_grid = (int *)malloc(sizeof(int) * (size_t)n_index);
     if (!r.num_nucs || !r.mats || !r.concs || !r.nuclide_grid || (n_index && !r.index_grid) ||
-        (t.grid_type == XS_UNIONIZED && !r.unionized_energy_array)) {
+        (gtype == XS_UNIONIZED && !r.unionized_energy_array)) {
         xs_simdata_free(&r);
         return fail(XS_ERR_OUT_OF_MEMORY, "host copies");
     }
@@ -413,7 +418,7 @@ xs_status xs_ctx_download(xs_ctx *ctx, xs_simdata *out)
     if (e == cudaSuccess && r.unionized_energy_array)
         e = cudaMemcpyAsync(r.unionized_energy_array, t.union_e, sizeof(double) * (size_t)t.n_union, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && n_index)
-        e = cudaMemcpyAsync(r.index_grid, t.index_grid, sizeof(int) * (size_t)n_index, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(r.index_grid, ctx->own_index, sizeof(int) * (size_t)n_index, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         xs_simdata_free(&r);
@@ -761,11 +766,6 @@ xs_status xs_adjoint_samples(xs_ctx *ctx, const xs_run_opts *opts, const double 
                           result);
 }
 
-xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opts *best)
-{
-    (void)ctx; (void)cache_path; (void)best;
-    return fail(XS_ERR_UNSUPPORTED, "autotuner is not built in this version");
-}
 
 xs_status xs_run_event_based_simulation(xs_inputs in, xs_simdata sd, int mype,
                                         unsigned long long *verification)

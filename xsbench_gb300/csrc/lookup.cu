@@ -432,9 +432,12 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
         ctx->device_bytes += need;
     }
     char key[256];
-    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d", arith, checked, first, count,
-             nb_log2, (const void *)in.energy, (const void *)in.mat, (void *)out.macro,
-             (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm);
+    // everything the captured launches bake in: options, pointers, grid view
+    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d/%d/%p/%p/%d", arith, checked,
+             first, count, nb_log2, (const void *)in.energy, (const void *)in.mat,
+             (void *)out.macro, (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm,
+             ctx->t.grid_type, (const void *)ctx->t.index_grid, (const void *)ctx->t.coarse,
+             ctx->t.hash_bins);
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
         cudaStream_t cap;

@@ -97,6 +97,13 @@ struct xs_ctx {
     cudaEvent_t pipe_event[2] = {nullptr, nullptr};
     void *pipe_buf = nullptr;
     size_t pipe_bytes = 0;
+    // grids the autotuner may switch to (owned through `allocations`)
+    const int *own_index = nullptr;           // the index grid the problem came with
+    const long long *base_coarse = nullptr;   // coarse keys built with the context
+    int base_n_coarse = 0;
+    int *tune_hash_index = nullptr;           // derived 10,000-bin hash grid
+    long long *tune_coarse = nullptr;         // derived coarse keys (nuclide grid)
+    int tune_n_coarse = 0;
 };
 
 namespace xsgb {
