@@ -88,8 +88,9 @@ def measured_peak_gbs():
 
 
 def profiled_traffic(workload, kernel):
-    """dram read+write bytes per lookup of the dominant kernel, from the ncu
-    summary committed under profiles/ (line 'dram_bytes_per_lookup: X')."""
+    """DRAM read+write bytes per lookup of one step of the path (for the plain
+    path: the tiled kernel plus its overflow pass), from the ncu summary
+    committed under profiles/ (line 'dram_bytes_per_lookup: X')."""
     name = os.path.join(ROOT, "profiles", f"{'k_plain' if kernel == 'plain' else 'k_batched_lookup'}_{workload}.md")
     try:
         for line in open(name):

@@ -326,6 +326,29 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
         t.mat_lo[m] = lo;
         t.mat_hi[m] = hi;
     }
+    {   // hot nuclides: most expected record accesses per lookup, within half of L2
+        double thr[kMaterials], prob[kMaterials];
+        pick_mat_thresholds(thr);
+        for (int m = 1; m < kMaterials; m++) prob[m] = thr[m] - thr[m - 1];
+        prob[0] = 1.0 - thr[kMaterials - 1];
+        std::vector<double> freq((size_t)in->n_isotopes, 0.0);
+        for (int m = 0; m < kMaterials; m++)
+            for (int j = 0; j < sd->num_nucs[m]; j++) freq[(size_t)sd->mats[m * sd->max_num_nucs + j]] += prob[m];
+        std::vector<int> order((size_t)in->n_isotopes);
+        for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return freq[(size_t)a] > freq[(size_t)b]; });
+        cudaDeviceProp prop;
+        size_t l2 = 64u << 20;
+        if (cudaGetDeviceProperties(&prop, device) == cudaSuccess && prop.l2CacheSize > 0) l2 = (size_t)prop.l2CacheSize;
+        const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = l2 / 2;
+        size_t used = 0;
+        std::memset(t.hot, 0, sizeof t.hot);
+        for (int n : order) {
+            if (n >= 512 || freq[(size_t)n] <= 0.0 || used + per > budget) continue;
+            t.hot[n >> 5] |= 1u << (n & 31);
+            used += per;
+        }
+    }
     {   // (material, position) pairs, and for each nuclide the pairs holding it
         t.pair_base[0] = 0;
         for (int m = 0; m < kMaterials; m++) t.pair_base[m + 1] = t.pair_base[m] + sd->num_nucs[m];

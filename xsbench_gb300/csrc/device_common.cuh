@@ -196,24 +196,52 @@ __device__ __forceinline__ long interval_hash(const Tables &t, long bin, int nuc
     return (lower == n_gp - 1) ? lower - 1 : lower;
 }
 
-// ------------------------------------------------------------- prefetch ---
-// TMA bulk prefetch of [p, p+bytes) into L2; p 16-byte aligned, bytes a
-// multiple of 16 (one instruction per 96-byte record or index-row span).
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
+// ------------------------------------------------------- L2 residency ---
+// Records of the nuclides most lookups touch are loaded and prefetched with an
+// evict_last policy so they stay in L2; the rest (the fuel-only nuclides'
+// records, the index rows) are streamed with evict_first.
+__device__ __forceinline__ unsigned long long policy_last()
 {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)),
-                 "r"(bytes)
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long policy_first()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ bool is_hot(const Tables &t, int nuc)
+{
+    return nuc < 512 && ((t.hot[nuc >> 5] >> (nuc & 31)) & 1u);
+}
+__device__ __forceinline__ unsigned long long record_policy(const Tables &t, int nuc)
+{
+    return is_hot(t, nuc) ? policy_last() : policy_first();
+}
+
+// ------------------------------------------------------------- prefetch ---
+// TMA bulk prefetch of [p, p+bytes) into L2 under an L2 policy; p 16-byte
+// aligned, bytes a multiple of 16 (one instruction per 96-byte record or
+// index-row span).
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes, unsigned long long pol)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(
+                     __cvta_generic_to_global(p)),
+                 "r"(bytes), "l"(pol)
                  : "memory");
 }
 
 // --------------------------------------------------------- interpolation ---
 // 32-byte read-only load that does not allocate in L1 (the records are
 // streamed; the material tables and index rows keep L1 to themselves).
-__device__ __forceinline__ void ld_v4(const double *p, double &a, double &b, double &c, double &d)
+__device__ __forceinline__ void ld_v4(const double *p, double &a, double &b, double &c, double &d,
+                                      unsigned long long pol)
 {
-    asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0,%1,%2,%3}, [%4];"
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
                  : "=d"(a), "=d"(b), "=d"(c), "=d"(d)
-                 : "l"(p));
+                 : "l"(p), "l"(pol));
 }
 
 // FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record, read
@@ -223,10 +251,11 @@ __device__ __forceinline__ void accumulate_fast(const Tables &t, int nuc, long k
                                                 double conc, double macro[5], double *S = nullptr)
 {
     const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * 6);
+    const unsigned long long pol = record_policy(t, nuc);
     double e_hi, h0, h1, h2, h3, h4, s0, s1, s2, s3, s4, e_lo;
-    ld_v4(r, e_hi, h0, h1, h2);
-    ld_v4(r + 4, h3, h4, s0, s1);
-    ld_v4(r + 8, s2, s3, s4, e_lo);
+    ld_v4(r, e_hi, h0, h1, h2, pol);
+    ld_v4(r + 4, h3, h4, s0, s1, pol);
+    ld_v4(r + 8, s2, s3, s4, e_lo, pol);
     (void)e_lo;
     const double d = e_hi - E;
     macro[0] = fma(fma(-d, s0, h0), conc, macro[0]);
@@ -299,7 +328,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
         // the material's span of the index row, 16-byte aligned
         const uintptr_t a = (uintptr_t)(irow + t.mat_lo[mat]) & ~(uintptr_t)15;
         const uintptr_t b = ((uintptr_t)(irow + t.mat_hi[mat] + 1) + 15) & ~(uintptr_t)15;
-        prefetch_l2((const void *)a, (unsigned)(b - a));
+        prefetch_l2((const void *)a, (unsigned)(b - a), policy_first());
     }
     const long top = t.n_gp - 1;
     int kr[2 * P];
@@ -310,7 +339,8 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
         if (q < n) {
             long k = kr[q];
             if (CHECKED && (k < 0 || k > top)) k = 0;
-            prefetch_l2(interval_bytes<ARITH>(t, ldg(&mrow[q]), k == top ? k - 1 : k), 96);
+            const int nq = ldg(&mrow[q]);
+            prefetch_l2(interval_bytes<ARITH>(t, nq, k == top ? k - 1 : k), 96, record_policy(t, nq));
         }
     for (int j0 = 0; j0 < n; j0 += 2 * P) {
 #pragma unroll
@@ -329,7 +359,9 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
                 if (jp < n) {
                     long kp = kr[(q + P) % (2 * P)];
                     if (CHECKED && (kp < 0 || kp > top)) kp = 0;
-                    prefetch_l2(interval_bytes<ARITH>(t, ldg(&mrow[jp]), kp == top ? kp - 1 : kp), 96);
+                    const int np = ldg(&mrow[jp]);
+                    prefetch_l2(interval_bytes<ARITH>(t, np, kp == top ? kp - 1 : kp), 96,
+                                record_policy(t, np));
                 }
                 const int nuc = ldg(&mrow[j]);
                 const double conc = ldg(&crow[j]);
