@@ -102,9 +102,9 @@ long or_grid_search_nuclide(long n, double quarry, const or_gridpoint *A, long l
 
 /* Simulation.c:241-323: micro XS of one nuclide.  idx is the union-grid index
  * (UNIONIZED) or the hash bin (HASH); unused for NUCLIDE. */
-static void or_micro_xs(double E, int nuc, long n_iso, long n_gp, const int *index_data,
-                        const or_gridpoint *grids, long idx, double xs[5], int grid_type,
-                        int hash_bins)
+static void or_micro_xs(double E, int nuc, long n_iso, long n_gp, const int *restrict index_data,
+                        const or_gridpoint *restrict grids, long idx, double *restrict xs,
+                        int grid_type, int hash_bins)
 {
     const or_gridpoint *nuc_grid = &grids[nuc * n_gp];
     const or_gridpoint *lo;
@@ -136,23 +136,30 @@ static void or_micro_xs(double E, int nuc, long n_iso, long n_gp, const int *ind
 }
 
 /* Simulation.c:326-375: macro XS = sum over the material's nuclides, in list order. */
-void or_macro_xs(const or_inputs *in, const or_simdata *sd, double E, int mat, double macro[5])
+void or_macro_xs(const or_inputs *in, const or_simdata *sd, double E, int mat, double *restrict macro)
 {
+    /* the reference passes these arrays as restrict parameters (Simulation.c:326-332) */
+    const int *restrict mats = sd->mats;
+    const double *restrict concs = sd->concs;
+    const int *restrict index_grid = sd->index_grid;
+    const or_gridpoint *restrict grid = sd->nuclide_grid;
+    const long n_iso = in->n_isotopes, n_gp = in->n_gridpoints;
+    const int grid_type = in->grid_type, hash_bins = in->hash_bins;
     long idx = -1;
     for (int k = 0; k < 5; k++) macro[k] = 0;
-    if (in->grid_type == OR_UNIONIZED)
-        idx = or_grid_search(in->n_isotopes * in->n_gridpoints, E, sd->unionized_energy_array);
-    else if (in->grid_type == OR_HASH) {
-        double du = 1.0 / in->hash_bins;
+    if (grid_type == OR_UNIONIZED)
+        idx = or_grid_search(n_iso * n_gp, E, sd->unionized_energy_array);
+    else if (grid_type == OR_HASH) {
+        double du = 1.0 / hash_bins;
         idx = (long)(E / du);
     }
     const int row = mat * sd->max_num_nucs;
-    for (int j = 0; j < sd->num_nucs[mat]; j++) {
+    const int nn = sd->num_nucs[mat];
+    for (int j = 0; j < nn; j++) {
         double xs[5];
-        int nuc = sd->mats[row + j];
-        double conc = sd->concs[row + j];
-        or_micro_xs(E, nuc, in->n_isotopes, in->n_gridpoints, sd->index_grid, sd->nuclide_grid,
-                    idx, xs, in->grid_type, in->hash_bins);
+        int nuc = mats[row + j];
+        double conc = concs[row + j];
+        or_micro_xs(E, nuc, n_iso, n_gp, index_grid, grid, idx, xs, grid_type, hash_bins);
         for (int k = 0; k < 5; k++) macro[k] += xs[k] * conc;
     }
 }

@@ -84,7 +84,7 @@ long or_grid_search(long n, double quarry, const double *A);
 long or_grid_search_nuclide(long n, double quarry, const or_gridpoint *A, long low, long high);
 
 /* One macroscopic lookup (Simulation.c:326-375). */
-void or_macro_xs(const or_inputs *in, const or_simdata *sd, double energy, int mat, double macro[5]);
+void or_macro_xs(const or_inputs *in, const or_simdata *sd, double energy, int mat, double *macro);
 
 /* argmax rule of the verification (Simulation.c:100-110): returns max_idx in 0..4. */
 int or_argmax5(const double macro[5]);
