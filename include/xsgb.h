@@ -162,8 +162,12 @@ xs_status xs_binary_read(const char *path, xs_simdata *out);
  * ownership of the host arrays. */
 xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out);
 
-/* Builds the problem directly on the device (the same tables as
- * xs_grid_init, bit for bit), with no host arrays and no upload. */
+/* Builds the problem directly on the device: the same tables as
+ * xs_grid_init (bit for bit), with no host arrays and no upload.  Replaces
+ * grid_init_do_not_profile (openmp-threading/GridInit.c:3) followed by
+ * move_simulation_data_to_device (cuda/GridInit.cu:4).  Returns
+ * XS_ERR_UNSUPPORTED for a unionized problem in which a nuclide draws the same
+ * energy twice (probability ~n_gridpoints^2 / 2^53; xs_grid_init handles it). */
 xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs_ctx **out);
 
 /* Copies the context's setup arrays back into host arrays shaped like

@@ -200,7 +200,11 @@ class HostProblem:
     def write(self, path: str):
         _check(lib().xs_binary_write(path.encode(), C.byref(self.sd)), "xs_binary_write")
 
-    def arrays(self) -> dict:
+    def arrays(self, copy: bool = False) -> dict:
+        """The setup arrays by reference name.  Without `copy` the arrays are
+        views of the C arrays and are valid only until close()."""
+        if copy:
+            return {k: np.array(v) for k, v in self.arrays().items()}
         sd = self.sd
         out = {"nuclide_grid": np.ctypeslib.as_array(
             C.cast(sd.nuclide_grid, C.POINTER(C.c_double)),

@@ -25,7 +25,8 @@ LIB_PATH = os.path.join(LIB_DIR, "libxsgb.so")
 EXE_PATH = os.path.join(LIB_DIR, "xsgb")
 
 CU_SOURCES = ["capi.cu", "setup_host.cu", "tables.cu", "lookup.cu", "lookup_unionized.cu",
-              "lookup_nuclide.cu", "lookup_hash.cu", "static_scratch.cu", "adjoint.cu", "tune.cu"]
+              "lookup_nuclide.cu", "lookup_hash.cu", "static_scratch.cu", "adjoint.cu", "tune.cu",
+              "setup_device.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

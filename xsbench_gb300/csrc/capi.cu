@@ -253,7 +253,12 @@ static xs_status check_problem(const xs_inputs *in, const xs_simdata *sd)
     return XS_OK;
 }
 
-static xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
+}  // extern "C"
+
+namespace xsgb {
+
+// A context with streams, events and run scratch, and no problem yet.
+xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
 {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
@@ -304,15 +309,12 @@ static xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
     return XS_OK;
 }
 
-xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out)
+// The material tables of a problem into an open context: the three arrays,
+// the nuclide span of each material, the nuclides whose records stay in L2
+// and the map nuclide -> (material, position) pairs.
+xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *sd)
 {
-    if (!out) return fail(XS_ERR_INVALID_ARGUMENT, "xs_ctx_create: out is NULL");
-    *out = nullptr;
-    xs_status s = check_problem(in, sd);
-    if (s != XS_OK) return s;
-    xs_ctx *ctx = nullptr;
-    s = ctx_open(in, device, &ctx);
-    if (s != XS_OK) return s;
+    xs_status s = XS_OK;
     Tables &t = ctx->t;
     t.max_nucs = sd->max_num_nucs;
     for (int m = 0; m < kMaterials; m++) {
@@ -339,7 +341,7 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return freq[(size_t)a] > freq[(size_t)b]; });
         cudaDeviceProp prop;
         size_t l2 = 64u << 20;
-        if (cudaGetDeviceProperties(&prop, device) == cudaSuccess && prop.l2CacheSize > 0) l2 = (size_t)prop.l2CacheSize;
+        if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess && prop.l2CacheSize > 0) l2 = (size_t)prop.l2CacheSize;
         const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = l2 / 2;
         size_t used = 0;
         std::memset(t.hot, 0, sizeof t.hot);
@@ -369,10 +371,28 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
             if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamSynchronize");
         }
     }
-    const long n_pts = in->n_isotopes * in->n_gridpoints;
     if (s == XS_OK) s = upload(ctx, sd->num_nucs, kMaterials, &t.num_nucs);
     if (s == XS_OK) s = upload(ctx, sd->mats, (size_t)sd->length_mats, &t.mats);
     if (s == XS_OK) s = upload(ctx, sd->concs, (size_t)sd->length_concs, &t.concs);
+    return s;
+}
+
+}  // namespace xsgb
+
+extern "C" {
+
+xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out)
+{
+    if (!out) return fail(XS_ERR_INVALID_ARGUMENT, "xs_ctx_create: out is NULL");
+    *out = nullptr;
+    xs_status s = check_problem(in, sd);
+    if (s != XS_OK) return s;
+    xs_ctx *ctx = nullptr;
+    s = ctx_open(in, device, &ctx);
+    if (s != XS_OK) return s;
+    Tables &t = ctx->t;
+    s = install_materials(ctx, in, sd);
+    const long n_pts = in->n_isotopes * in->n_gridpoints;
     if (s == XS_OK) s = upload(ctx, sd->nuclide_grid, (size_t)n_pts, &t.grid);
     if (s == XS_OK && in->grid_type == XS_UNIONIZED) {
         t.n_union = sd->length_unionized_energy_array;
@@ -391,14 +411,6 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
     ctx->base_n_coarse = t.n_coarse;
     *out = ctx;
     return XS_OK;
-}
-
-xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs_ctx **out)
-{
-    (void)in;
-    (void)device;
-    (void)out;
-    return fail(XS_ERR_UNSUPPORTED, "device-side problem setup is not built in this version");
 }
 
 xs_status xs_ctx_download(xs_ctx *ctx, xs_simdata *out)

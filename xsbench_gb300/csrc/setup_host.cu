@@ -100,6 +100,49 @@ static long search_points(const xs_gridpoint *A, double q, long lo, long hi)
     return lo;
 }
 
+// Materials.c:7-117
+xs_status load_materials(long n_iso, xs_simdata *sd)
+{
+    static const int rest[11] = {5, 4, 4, 27, 21, 21, 21, 21, 21, 9, 9};
+    static const int fuel34[34] = {58, 59, 60, 61, 40, 42, 43, 44, 45, 46, 1,  2,
+                                   3,  7,  8,  9,  10, 29, 57, 47, 48, 0,  62, 15,
+                                   33, 34, 52, 53, 54, 55, 56, 18, 23, 41};
+    static const int clad[5] = {63, 64, 65, 66, 67};
+    static const int water[4] = {24, 41, 4, 5};
+    static const int rpv[27] = {19, 20, 21, 22, 35, 36, 37, 38, 39, 25, 27, 28, 29, 30,
+                                31, 32, 26, 49, 50, 51, 11, 12, 13, 14, 6,  16, 17};
+    static const int refl[21] = {24, 41, 4, 5, 19, 20, 21, 22, 35, 36, 37,
+                                 38, 39, 25, 49, 50, 51, 11, 12, 13, 14};
+    static const int fa_end[9] = {24, 41, 4, 5, 63, 64, 65, 66, 67};
+    static const int *const lists[kMaterials] = {nullptr, clad, water, water, rpv,    refl,
+                                                 refl,    refl, refl,  refl,  fa_end, fa_end};
+    int nn[kMaterials];
+    nn[0] = (n_iso == 68) ? 34 : 321;
+    for (int m = 1; m < kMaterials; m++) nn[m] = rest[m - 1];
+    int mx = 0;
+    for (int m = 0; m < kMaterials; m++) mx = std::max(mx, nn[m]);
+    // the lists name nuclides up to 67 (small) or 354 (large)
+    const int highest = (n_iso == 68) ? 67 : 354;
+    if (n_iso <= highest)
+        return fail(XS_ERR_INVALID_ARGUMENT, "n_isotopes %ld: the material lists need 68 (small) or at least 355 nuclides", n_iso);
+    sd->length_num_nucs = kMaterials;
+    sd->max_num_nucs = mx;
+    sd->length_mats = kMaterials * mx;
+    sd->length_concs = sd->length_mats;
+    sd->num_nucs = (int *)malloc(sizeof nn);
+    sd->mats = (int *)calloc((size_t)sd->length_mats, sizeof(int));
+    sd->concs = (double *)calloc((size_t)sd->length_concs, sizeof(double));
+    if (!sd->num_nucs || !sd->mats || !sd->concs) return fail(XS_ERR_OUT_OF_MEMORY, "material tables");
+    std::memcpy(sd->num_nucs, nn, sizeof nn);
+    for (int j = 0; j < nn[0]; j++) sd->mats[j] = j < 34 ? fuel34[j] : 68 + (j - 34);
+    for (int m = 1; m < kMaterials; m++)
+        std::memcpy(sd->mats + m * mx, lists[m], sizeof(int) * (size_t)nn[m]);
+    unsigned long long seed = kStartingSeed * kStartingSeed;  // Materials.c:101
+    for (int m = 0; m < kMaterials; m++)
+        for (int j = 0; j < nn[m]; j++) sd->concs[m * mx + j] = lcg_next(seed);
+    return XS_OK;
+}
+
 }  // namespace xsgb
 
 using namespace xsgb;
@@ -214,49 +257,6 @@ void xs_simdata_free(xs_simdata *sd)
     free(sd->p_energy_samples);
     free(sd->mat_samples);
     std::memset(sd, 0, sizeof *sd);
-}
-
-// Materials.c:7-117
-static xs_status load_materials(long n_iso, xs_simdata *sd)
-{
-    static const int rest[11] = {5, 4, 4, 27, 21, 21, 21, 21, 21, 9, 9};
-    static const int fuel34[34] = {58, 59, 60, 61, 40, 42, 43, 44, 45, 46, 1,  2,
-                                   3,  7,  8,  9,  10, 29, 57, 47, 48, 0,  62, 15,
-                                   33, 34, 52, 53, 54, 55, 56, 18, 23, 41};
-    static const int clad[5] = {63, 64, 65, 66, 67};
-    static const int water[4] = {24, 41, 4, 5};
-    static const int rpv[27] = {19, 20, 21, 22, 35, 36, 37, 38, 39, 25, 27, 28, 29, 30,
-                                31, 32, 26, 49, 50, 51, 11, 12, 13, 14, 6,  16, 17};
-    static const int refl[21] = {24, 41, 4, 5, 19, 20, 21, 22, 35, 36, 37,
-                                 38, 39, 25, 49, 50, 51, 11, 12, 13, 14};
-    static const int fa_end[9] = {24, 41, 4, 5, 63, 64, 65, 66, 67};
-    static const int *const lists[kMaterials] = {nullptr, clad, water, water, rpv,    refl,
-                                                 refl,    refl, refl,  refl,  fa_end, fa_end};
-    int nn[kMaterials];
-    nn[0] = (n_iso == 68) ? 34 : 321;
-    for (int m = 1; m < kMaterials; m++) nn[m] = rest[m - 1];
-    int mx = 0;
-    for (int m = 0; m < kMaterials; m++) mx = std::max(mx, nn[m]);
-    // the lists name nuclides up to 67 (small) or 354 (large)
-    const int highest = (n_iso == 68) ? 67 : 354;
-    if (n_iso <= highest)
-        return fail(XS_ERR_INVALID_ARGUMENT, "n_isotopes %ld: the material lists need 68 (small) or at least 355 nuclides", n_iso);
-    sd->length_num_nucs = kMaterials;
-    sd->max_num_nucs = mx;
-    sd->length_mats = kMaterials * mx;
-    sd->length_concs = sd->length_mats;
-    sd->num_nucs = (int *)malloc(sizeof nn);
-    sd->mats = (int *)calloc((size_t)sd->length_mats, sizeof(int));
-    sd->concs = (double *)calloc((size_t)sd->length_concs, sizeof(double));
-    if (!sd->num_nucs || !sd->mats || !sd->concs) return fail(XS_ERR_OUT_OF_MEMORY, "material tables");
-    std::memcpy(sd->num_nucs, nn, sizeof nn);
-    for (int j = 0; j < nn[0]; j++) sd->mats[j] = j < 34 ? fuel34[j] : 68 + (j - 34);
-    for (int m = 1; m < kMaterials; m++)
-        std::memcpy(sd->mats + m * mx, lists[m], sizeof(int) * (size_t)nn[m]);
-    unsigned long long seed = kStartingSeed * kStartingSeed;  // Materials.c:101
-    for (int m = 0; m < kMaterials; m++)
-        for (int j = 0; j < nn[m]; j++) sd->concs[m * mx + j] = lcg_next(seed);
-    return XS_OK;
 }
 
 xs_status xs_grid_init(const xs_inputs *in, xs_simdata *out)

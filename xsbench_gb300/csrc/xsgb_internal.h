@@ -183,5 +183,11 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
 
 // host setup (setup_host.cu)
 void pick_mat_thresholds(double out[kMaterials]);
+// the 12 materials of Materials.c:7-117 (host arrays, freed by xs_simdata_free)
+xs_status load_materials(long n_iso, xs_simdata *sd);
+
+// context assembly (capi.cu)
+xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out);
+xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *sd);
 
 }  // namespace xsgb
