@@ -250,8 +250,10 @@ def main():
                     help="override gridpoints per nuclide (a smaller case of the workload, for profiling)")
     ap.add_argument("--buckets", type=int, default=0, help="batched: energy buckets per material")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--adjoint", action="store_true",
-                    help="also time forward+adjoint (xs_run_adjoint, device arrays) per step")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the forward+adjoint side measurement (xs_run_adjoint, device arrays)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the side measurement of the other kernel on the same workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     args = ap.parse_args()
@@ -336,8 +338,32 @@ def main():
     e2e_ok = re.verification == last.verification
     e2e_value = world * N / statistics.median(e2e_t)
 
+    # the other lookup kernel on the same workload and context (same hash)
+    other = None
+    if not args.no_batched:
+        okind = "batched" if args.kernel == "plain" else "plain"
+        okw = dict(kw, kernel=okind, tile=0, buckets=0)
+        for _ in range(max(3, args.warmup)):
+            ctx.run_event(async_=True, **okw)
+        ctx.sync()
+        o0 = torch.cuda.Event(enable_timing=True)
+        o1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        o0.record(stream)
+        for _ in range(args.steps):
+            ctx.run_event(async_=True, **okw)
+        o1.record(stream)
+        torch.cuda.synchronize()
+        ro = ctx.sync()
+        t_o = o0.elapsed_time(o1) / 1e3
+        other = {"kernel": okind, "value": N * args.steps / t_o, "unit": UNIT,
+                 "ms_per_step": t_o / args.steps * 1e3,
+                 "vs_value": (N * args.steps / t_o) / (N * args.steps / t),
+                 "hash_ok": ro.hash == last.hash,
+                 "union_table": bool(okind == "batched" and ctx.union_table_bytes > 0)}
+
     adj = None
-    if args.adjoint:
+    if not args.no_adjoint:
         g = torch.randn((N, 5), dtype=torch.float64, device="cuda",
                         generator=torch.Generator(device="cuda").manual_seed(1234))
         d_e = torch.empty(N, dtype=torch.float64, device="cuda")
@@ -384,7 +410,9 @@ def main():
                        "l2": "inputs larger than L2 (tables > 129 MB), no flush",
                        "parallelism": f"shards x{world} (event index ranges)",
                        "hash_ok": bool(hash_ok), "hash": last.hash,
-                       "setup_s": round(t_setup, 2)},
+                       "setup_s": round(t_setup, 2),
+                       "union_table_gb": round(ctx.union_table_bytes / 1e9, 1),
+                       "device_gb": round(ctx.device_bytes / 1e9, 1)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_lookup": bpl,
@@ -394,6 +422,7 @@ def main():
                     "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",
                     "verification_matches": bool(e2e_ok)},
             "gpu_launches": launches,
+            "other_kernel": other,
             "forward_adjoint": adj,
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -180,6 +180,17 @@ void xs_ctx_destroy(xs_ctx *ctx);
 /* Bytes of device memory the context holds. */
 size_t xs_ctx_device_bytes(const xs_ctx *ctx);
 
+/* Bytes of the context's union table (0: not built).  For a unionized problem
+ * the context reconstructs every nuclide's cross sections on the union grid:
+ * per material and union row, each nuclide's five xs at the row energy and
+ * the slopes of its interval (80 bytes), so a FAST lookup reads its
+ * material's entries of one row contiguously instead of an index entry and a
+ * 96-byte interval per nuclide.  Built at context creation when the device
+ * has the room (n_union x sum(num_nucs) x 80 bytes, 155 GB for the large
+ * problem, plus 24 GiB to spare); XSGB_UNION_TABLE=0 in the environment
+ * disables it.  No reference counterpart. */
+size_t xs_ctx_union_table_bytes(const xs_ctx *ctx);
+
 /* Fills opts with defaults (PLAIN, FAST, all lookups, tuned shapes). */
 void xs_run_opts_init(xs_run_opts *opts);
 

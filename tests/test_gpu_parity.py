@@ -77,6 +77,33 @@ def test_tiny_against_reference(name, kernel, arith):
         assert rel_err(macro, ref) <= REL_TOL
 
 
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "tiny_nuclide"])
+@pytest.mark.parametrize("lanes", ["1", "2", "4"])
+@pytest.mark.parametrize("table", ["1", "0"])
+def test_fuel_lane_split(monkeypatch, name, lanes, table):
+    """The plain and batched kernels with the fuel nuclides split over 1, 2 or
+    4 lanes per lookup (FAST arithmetic; the partial sums are added in a fixed
+    tree), with and without the union table (unionized grid): the same argmax
+    vector and hash as the reference, macro_xs within REL_TOL, and
+    bit-identical results run to run."""
+    monkeypatch.setenv("XSGB_FUEL_LANES", lanes)
+    monkeypatch.setenv("XSGB_BATCHED_FUEL_LANES", lanes)
+    monkeypatch.setenv("XSGB_UNION_TABLE", table)
+    g = golden_json("full_" + name)
+    inp = product_inputs(name)
+    with oracle.Problem(oracle_config(name)) as o:
+        ref = o.run_event(want_macro=True)["macro"]
+    with X.grid_init(inp) as prob, X.Context(inp, prob) as ctx:
+        assert (ctx.union_table_bytes > 0) == (table == "1" and name == "tiny_unionized")
+        for kernel in ("plain", "batched"):
+            r, macro, idx = run(ctx, g["lookups"], kernel=kernel, arith="fast")
+            r2, macro2, _ = run(ctx, g["lookups"], kernel=kernel, arith="fast")
+            assert r.verification == g["verification"] == r2.verification, kernel
+            assert sha(idx) == g["sha256_max_idx"], kernel
+            assert np.array_equal(macro, macro2), kernel
+            assert rel_err(macro, ref) <= REL_TOL, kernel
+
+
 @pytest.mark.parametrize("name", ["small_unionized", "small_hash", "small_nuclide",
                                   "large_unionized", "large_hash", "large_nuclide"])
 def test_full_size_against_reference(name):

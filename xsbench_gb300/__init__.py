@@ -92,6 +92,7 @@ _SIGNATURES = {
     "xs_ctx_download": ([C.c_void_p, _P(SimData)], C.c_int),
     "xs_ctx_destroy": ([C.c_void_p], None),
     "xs_ctx_device_bytes": ([C.c_void_p], C.c_size_t),
+    "xs_ctx_union_table_bytes": ([C.c_void_p], C.c_size_t),
     "xs_ctx_sync": ([C.c_void_p, _P(RunResult)], C.c_int),
     "xs_run_opts_init": ([_P(RunOpts)], None),
     "xs_run_event": ([C.c_void_p, _P(RunOpts), C.c_void_p, C.c_void_p, _P(RunResult)], C.c_int),
@@ -290,6 +291,12 @@ class Context:
     @property
     def device_bytes(self) -> int:
         return int(lib().xs_ctx_device_bytes(self._h))
+
+    @property
+    def union_table_bytes(self) -> int:
+        """Bytes of the union table (0: the lookups read index entries and
+        interval records)."""
+        return int(lib().xs_ctx_union_table_bytes(self._h))
 
     def run_event(self, macro_out=None, max_idx_out=None, **kw) -> Result:
         o = _opts(**kw)

@@ -529,6 +529,8 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     l.out_idx = nullptr;
     l.verif = ctx->s.verification;
     l.err = ctx->s.error;
+    l.fuel_lanes = 1;
+    l.table = 0;
     s = launch_adjoint_energy(ctx, st, l, sg, d_energy);
     if (s != XS_OK) return s;
 

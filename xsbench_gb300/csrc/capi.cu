@@ -195,6 +195,8 @@ void xs_run_opts_init(xs_run_opts *o)
 
 size_t xs_ctx_device_bytes(const xs_ctx *ctx) { return ctx ? ctx->device_bytes : 0; }
 
+size_t xs_ctx_union_table_bytes(const xs_ctx *ctx) { return ctx ? ctx->union_table_bytes : 0; }
+
 void xs_ctx_destroy(xs_ctx *ctx)
 {
     if (!ctx) return;
@@ -271,6 +273,12 @@ xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
     if (prop.major != 10 || prop.minor != 3)
         return fail(XS_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", device, prop.major, prop.minor);
     XS_CUDA(cudaSetDevice(device));
+    if (const char *env = getenv("XSGB_L2_FETCH")) {
+        // the L2 fetch-granularity hint of this process's context on the device
+        const int v = atoi(env);
+        if (v >= 0 && v <= 128) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)v);
+        cudaGetLastError();
+    }
     xs_ctx *ctx = new xs_ctx();
     ctx->device = device;
     ctx->inputs = *in;
@@ -342,7 +350,12 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
         cudaDeviceProp prop;
         size_t l2 = 64u << 20;
         if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess && prop.l2CacheSize > 0) l2 = (size_t)prop.l2CacheSize;
-        const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = l2 / 2;
+        double frac = 0.5;
+        if (const char *env = getenv("XSGB_HOT_FRACTION")) {
+            const double v = atof(env);
+            if (v >= 0.0 && v <= 1.0) frac = v;
+        }
+        const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = (size_t)(l2 * frac);
         size_t used = 0;
         std::memset(t.hot, 0, sizeof t.hot);
         for (int n : order) {
@@ -370,6 +383,20 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
             cudaError_t e = cudaStreamSynchronize(ctx->stream);
             if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamSynchronize");
         }
+    }
+    // a fuel list this long is split over 4 lanes per lookup in the plain
+    // kernel (FAST arithmetic) and over 2 in the batched kernel when it reads
+    // the union table (set by build_union_table); XSGB_FUEL_LANES and
+    // XSGB_BATCHED_FUEL_LANES = 1, 2 or 4 override
+    for (int m = 0; m < kMaterials; m++) ctx->num_nucs_host[m] = sd->num_nucs[m];
+    ctx->fuel_lanes = sd->num_nucs[0] >= 64 ? 4 : 1;
+    if (const char *env = getenv("XSGB_FUEL_LANES")) {
+        const int v = atoi(env);
+        if (v == 1 || v == 2 || v == 4) ctx->fuel_lanes = v;
+    }
+    if (const char *env = getenv("XSGB_BATCHED_FUEL_LANES")) {
+        const int v = atoi(env);
+        if (v == 1 || v == 2 || v == 4) ctx->batched_fuel_lanes = v;
     }
     if (s == XS_OK) s = upload(ctx, sd->num_nucs, kMaterials, &t.num_nucs);
     if (s == XS_OK) s = upload(ctx, sd->mats, (size_t)sd->length_mats, &t.mats);
@@ -403,6 +430,7 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
         ctx->own_index = t.index_grid;
     }
     if (s == XS_OK) s = build_derived_tables(ctx);
+    if (s == XS_OK) s = build_union_table(ctx);
     if (s != XS_OK) {
         xs_ctx_destroy(ctx);
         return s;

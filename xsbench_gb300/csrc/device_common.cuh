@@ -244,6 +244,16 @@ __device__ __forceinline__ void ld_v4(const double *p, double &a, double &b, dou
                  : "l"(p), "l"(pol));
 }
 
+// 16-byte streaming load (no L1 allocation) under an L2 policy.
+__device__ __forceinline__ double2 ld_v2(const double2 *p, unsigned long long pol)
+{
+    double2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;"
+                 : "=d"(v.x), "=d"(v.y)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+
 // FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record, read
 // with three 32-byte loads (a record is three aligned sectors).
 template <bool DE = false>
@@ -315,56 +325,87 @@ __device__ __forceinline__ const void *interval_bytes(const Tables &t, int nuc, 
 // UNIONIZED nuclide loop, software-pipelined: the index entry of nuclide j+2P
 // is loaded and the 96-byte interval of nuclide j+P is prefetched into L2 while
 // nuclide j is interpolated, so a lane keeps three gathers in flight instead
-// of waiting on each dependent pair.  Accumulation order is the reference's.
-template <int ARITH, bool CHECKED, bool DE>
+// of waiting on each dependent pair.  The lane runs the nuclides
+// j = q0, q0 + S, q0 + 2S, ... of the material (S = 1: all of them, in the
+// reference's order).
+//
+// TABLE (FAST arithmetic, union table built): the lane reads its nuclides'
+// entries of the row instead of index entries and interval records.
+template <int ARITH, bool CHECKED, bool DE, bool TABLE = false>
 __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, int mat, int n,
                                                    const int *mrow, const double *crow,
-                                                   double macro[5], int *err, double *S)
+                                                   double macro[5], int *err, double *S,
+                                                   int q0 = 0, int stride = 1)
 {
-    constexpr int P = 2;
     const long row = union_row(t, E);
+    if (TABLE) {
+        // the material's entries of this row are contiguous, 80 bytes per
+        // nuclide (five pairs (v, s)); xs = v + s * (E - u_row), the
+        // interval's line evaluated at E
+        const double dl = E - ldg(&t.union_e[row]);
+        const double2 *blk = t.utab[mat] + row * n * 5;
+        const unsigned long long pol = policy_first();
+#pragma unroll 4
+        for (int j = q0; j < n; j += stride) {
+            const double2 *p = blk + (long)j * 5;
+            const double2 a0 = ld_v2(p, pol), a1 = ld_v2(p + 1, pol), a2 = ld_v2(p + 2, pol);
+            const double2 a3 = ld_v2(p + 3, pol), a4 = ld_v2(p + 4, pol);
+            const double conc = ldg(&crow[j]);
+            macro[0] = fma(fma(a0.y, dl, a0.x), conc, macro[0]);
+            macro[1] = fma(fma(a1.y, dl, a1.x), conc, macro[1]);
+            macro[2] = fma(fma(a2.y, dl, a2.x), conc, macro[2]);
+            macro[3] = fma(fma(a3.y, dl, a3.x), conc, macro[3]);
+            macro[4] = fma(fma(a4.y, dl, a4.x), conc, macro[4]);
+        }
+        return;
+    }
+    constexpr int P = 2;
     const int *irow = t.index_grid + row * t.n_iso;
-    {
+    if (q0 == 0) {
         // the material's span of the index row, 16-byte aligned
         const uintptr_t a = (uintptr_t)(irow + t.mat_lo[mat]) & ~(uintptr_t)15;
         const uintptr_t b = ((uintptr_t)(irow + t.mat_hi[mat] + 1) + 15) & ~(uintptr_t)15;
         prefetch_l2((const void *)a, (unsigned)(b - a), policy_first());
     }
+    // this lane's nuclides: positions q0 + stride * i, i < nl
+    const int nl = n > q0 ? (n - q0 + stride - 1) / stride : 0;
+    mrow += q0;
+    crow += q0;
     const long top = t.n_gp - 1;
     int kr[2 * P];
 #pragma unroll
-    for (int q = 0; q < 2 * P; q++) kr[q] = (q < n) ? ldg(&irow[ldg(&mrow[q])]) : 0;
+    for (int q = 0; q < 2 * P; q++) kr[q] = (q < nl) ? ldg(&irow[ldg(&mrow[q * stride])]) : 0;
 #pragma unroll
     for (int q = 0; q < P; q++)
-        if (q < n) {
+        if (q < nl) {
             long k = kr[q];
             if (CHECKED && (k < 0 || k > top)) k = 0;
-            const int nq = ldg(&mrow[q]);
+            const int nq = ldg(&mrow[q * stride]);
             prefetch_l2(interval_bytes<ARITH>(t, nq, k == top ? k - 1 : k), 96, record_policy(t, nq));
         }
-    for (int j0 = 0; j0 < n; j0 += 2 * P) {
+    for (int j0 = 0; j0 < nl; j0 += 2 * P) {
 #pragma unroll
         for (int q = 0; q < 2 * P; q++) {
             const int j = j0 + q;
-            if (j < n) {
+            if (j < nl) {
                 long k = kr[q];
                 if (CHECKED && (k < 0 || k > top)) {
-                    report(err, XS_ERR_DATA, row, ldg(&mrow[j]));
+                    report(err, XS_ERR_DATA, row, ldg(&mrow[j * stride]));
                     k = 0;
                 }
                 if (k == top) k -= 1;
                 const int jn = j + 2 * P;
-                if (jn < n) kr[q] = ldg(&irow[ldg(&mrow[jn])]);
+                if (jn < nl) kr[q] = ldg(&irow[ldg(&mrow[jn * stride])]);
                 const int jp = j + P;
-                if (jp < n) {
+                if (jp < nl) {
                     long kp = kr[(q + P) % (2 * P)];
                     if (CHECKED && (kp < 0 || kp > top)) kp = 0;
-                    const int np = ldg(&mrow[jp]);
+                    const int np = ldg(&mrow[jp * stride]);
                     prefetch_l2(interval_bytes<ARITH>(t, np, kp == top ? kp - 1 : kp), 96,
                                 record_policy(t, np));
                 }
-                const int nuc = ldg(&mrow[j]);
-                const double conc = ldg(&crow[j]);
+                const int nuc = ldg(&mrow[j * stride]);
+                const double conc = ldg(&crow[j * stride]);
                 if (ARITH == XS_ARITH_EXACT)
                     accumulate_exact(t, nuc, k, E, conc, macro);
                 else
@@ -377,9 +418,12 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
 // ------------------------------------------------------------ one lookup ---
 // calculate_macro_xs (Simulation.c:326-375) for one (E, mat).
 // With DE, S[5] receives d macro_xs / dE (the adjoint's energy derivative).
-template <int GRID, int ARITH, bool CHECKED, bool DE = false>
+// With stride > 1 the call computes the partial sum over the nuclides
+// j = q0, q0 + stride, ... only (one of `stride` lanes sharing the lookup).
+template <int GRID, int ARITH, bool CHECKED, bool DE = false, bool TABLE = false>
 __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, double macro[5],
-                                         int *err, double *S = nullptr)
+                                         int *err, double *S = nullptr, int q0 = 0,
+                                         int stride = 1)
 {
 #pragma unroll
     for (int c = 0; c < 5; c++) macro[c] = 0.0;
@@ -391,7 +435,8 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
     const int *mrow = t.mats + mat * t.max_nucs;
     const double *crow = t.concs + mat * t.max_nucs;
     if (GRID == XS_UNIONIZED) {
-        macro_xs_unionized<ARITH, CHECKED, DE>(t, E, mat, n, mrow, crow, macro, err, S);
+        macro_xs_unionized<ARITH, CHECKED, DE, TABLE>(t, E, mat, n, mrow, crow, macro, err, S, q0,
+                                                      stride);
         return;
     }
     long row = 0;
@@ -411,7 +456,7 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
         q = order_key(E);
     }
 #pragma unroll 2
-    for (int j = 0; j < n; j++) {
+    for (int j = q0; j < n; j += stride) {
         const int nuc = ldg(&mrow[j]);
         const double conc = ldg(&crow[j]);
         long k;

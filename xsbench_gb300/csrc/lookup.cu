@@ -245,6 +245,7 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
     a.ovf_E = ps ? ps->E : nullptr;
     a.ovf_id = ps ? ps->id : nullptr;
     a.ovf_cap = ps ? ps->cap : 0;
+    a.fuel_lanes = ctx->fuel_lanes;
     if (ps) {
         XS_CUDA(cudaMemsetAsync(ps->cnt, 0, 256, st));  // counts, layout, queue
     }
@@ -264,6 +265,8 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
         l.out_idx = out.max_idx;
         l.verif = ctx->s.verification;
         l.err = ctx->s.error;
+        l.fuel_lanes = ctx->fuel_lanes;  // the plain kernel's arithmetic, lookup for lookup
+        l.table = 0;
         XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
                                           ctx->sm_count * ctx->batched_blocks_per_sm, l));
         if (launches) *launches += 2;
@@ -321,6 +324,8 @@ static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int ch
     l.out_idx = out.max_idx;
     l.verif = ctx->s.verification;
     l.err = ctx->s.error;
+    l.fuel_lanes = ctx->batched_fuel_lanes;
+    l.table = 1;
     XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
                                       ctx->sm_count * ctx->batched_blocks_per_sm, l));
     if (launches) *launches += 4;
@@ -398,6 +403,8 @@ xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first
     l.out_idx = out.max_idx;
     l.verif = b.verification;
     l.err = b.error;
+    l.fuel_lanes = ctx->batched_fuel_lanes;
+    l.table = 1;
     XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, 0,
                                       ctx->sm_count * ctx->batched_blocks_per_sm, l));
     return XS_OK;
@@ -433,11 +440,11 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
     }
     char key[256];
     // everything the captured launches bake in: options, pointers, grid view
-    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d/%d/%p/%p/%d", arith, checked,
+    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d/%d/%p/%p/%d/%d", arith, checked,
              first, count, nb_log2, (const void *)in.energy, (const void *)in.mat,
              (void *)out.macro, (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm,
              ctx->t.grid_type, (const void *)ctx->t.index_grid, (const void *)ctx->t.coarse,
-             ctx->t.hash_bins);
+             ctx->t.hash_bins, ctx->batched_fuel_lanes * 2 + (ctx->t.utab[0] != nullptr));
     auto it = ctx->graphs.find(key);
     if (it == ctx->graphs.end()) {
         cudaStream_t cap;

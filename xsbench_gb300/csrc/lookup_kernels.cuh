@@ -13,6 +13,7 @@ constexpr int kWarps = kBlock / 32;
 #define XSGB_PLAIN_MIN_BLOCKS 4      // resident blocks per SM the compiler must allow
 #endif
 
+
 // Arguments of the plain (tiled) lookup kernel.
 struct PlainArgs {
     long first, count;
@@ -29,6 +30,11 @@ struct PlainArgs {
     double *ovf_E;               // [12 * ovf_cap]
     int *ovf_id;                 // [12 * ovf_cap]
     int ovf_cap;                 // entries per material
+    // lanes per fuel (material 0) lookup: 1, or with FAST arithmetic 2 or 4,
+    // each lane summing every fuel_lanes-th nuclide (the partial sums are
+    // added in a fixed tree), so a fuel chunk is 32 / fuel_lanes lookups and
+    // the block's warps finish their tile together
+    int fuel_lanes;
 };
 
 // A material-segmented list of lookups (the batched sort, or the plain
@@ -47,6 +53,8 @@ struct ListArgs {
     unsigned char *out_idx;
     unsigned long long *verif;
     int *err;
+    int fuel_lanes;              // lanes per fuel lookup (PlainArgs::fuel_lanes)
+    int table;                   // 1: read the union table when there is one (FAST)
 };
 
 // Adds the per-lane verification counts of a block into *verif (one atomic).
@@ -84,13 +92,40 @@ __device__ __forceinline__ bool sample_at(const Tables &t, const double *in_E, c
 }
 
 // One lookup of the event batch: macro_xs, argmax, outputs.
-template <int GRID, int ARITH, bool CHECKED>
+template <int GRID, int ARITH, bool CHECKED, bool TABLE>
 __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, int m, long o,
                                                      double *out_macro, unsigned char *out_idx,
                                                      int *err)
 {
     double macro[5];
-    macro_xs<GRID, ARITH, CHECKED>(t, E, m, macro, err);
+    macro_xs<GRID, ARITH, CHECKED, false, TABLE>(t, E, m, macro, err);
+    const int arg = argmax5(macro);
+    if (out_macro) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
+    }
+    if (out_idx) out_idx[o] = (unsigned char)arg;
+    return (unsigned)(arg + 1);
+}
+
+// One fuel (material 0) lookup spread over L lanes, FAST arithmetic: lane q
+// sums the nuclides j = q, q + L, ...; the partial sums are added in the fixed
+// tree (q0 + q1) + (q2 + q3), which gives the same bits on every lane of the
+// lookup.  Every lane of the warp calls this (shuffles); `live` is the same on
+// the L lanes of a lookup.  Returns argmax+1 on the lookup's lane q == 0.
+template <int GRID, bool CHECKED, bool TABLE>
+__device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool live, double E,
+                                                           long o, int q, int L,
+                                                           double *out_macro,
+                                                           unsigned char *out_idx, int *err)
+{
+    double macro[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (live) macro_xs<GRID, XS_ARITH_FAST, CHECKED, false, TABLE>(t, E, 0, macro, err, nullptr, q, L);
+    for (int s = 1; s < L; s <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) macro[k] += __shfl_xor_sync(0xffffffffu, macro[k], s);
+    }
+    if (!live || q != 0) return 0;
     const int arg = argmax5(macro);
     if (out_macro) {
 #pragma unroll
@@ -103,11 +138,18 @@ __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, 
 // ---------------------------------------------------------------- PLAIN ---
 // One block = one tile of `tile` consecutive lookups.  The block samples them,
 // counting-sorts their ids by material in shared memory, then its warps pull
-// 32-lookup chunks, fuel first, from a shared-memory queue and run one lookup
-// per lane, so a warp never mixes materials.  With overflow queues the last,
-// partial chunk of every material goes to the queue instead of running with
-// idle lanes.
-template <int GRID, int ARITH, bool CHECKED, bool SAMPLES>
+// chunks, fuel first, from a shared-memory queue, so a warp never mixes
+// materials: a chunk of another material is 32 lookups, one per lane; a fuel
+// chunk is 32 / fuel_lanes lookups with fuel_lanes lanes each.  With overflow
+// queues the last, partial 32 lookups of every material go to the queue
+// instead of running with idle lanes.
+//
+// The plain kernel reads index entries and interval records, never the union
+// table: its lookups are in random energy order, so each lane would stream a
+// different row of a table of ~155 GB, and the page-translation misses of that
+// pattern cost more than the bytes it saves (the batched kernel, whose warps
+// read neighbouring rows, uses it).
+template <int GRID, int ARITH, bool CHECKED, bool SAMPLES, bool TABLE = false>
 __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables t, PlainArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -194,20 +236,34 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
 
     unsigned long long mine = 0;
     const int lane = tid & 31;
-    const int nchunks = seg[kMaterials] >> 5;
+    // fuel chunks of 32 / L lookups first, then 32-lookup chunks of the rest
+    const int L = (ARITH == XS_ARITH_FAST) ? a.fuel_lanes : 1;
+    const int fuel_v = L > 1 ? seg[1] : 0;
+    const int nfuel = fuel_v / (32 / L);
+    const int nchunks = nfuel + ((seg[kMaterials] - fuel_v) >> 5);
     for (;;) {
         unsigned int c = 0;
         if (lane == 0) c = atomicAdd(&qhead, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
         if ((int)c >= nchunks) break;
-        const int p = (int)c * 32 + lane;
+        if (ARITH == XS_ARITH_FAST && (int)c < nfuel) {
+            const int q = lane & (L - 1);
+            const int p = (int)c * (32 / L) + lane / L;
+            const bool live = p < (overflow ? (cnt[0] & ~31) : cnt[0]);
+            const int l = live ? perm[p] : 0;
+            mine += split_lookup_and_store<GRID, CHECKED, TABLE>(t, live, sE[l], base + l, q, L,
+                                                                 a.out_macro, a.out_idx, a.err);
+            continue;
+        }
+        const int cv = (int)c - nfuel + (fuel_v >> 5);
+        const int p = cv * 32 + lane;
         int m = 0;
-        while (seg[m + 1] <= (int)c * 32) m++;
+        while (seg[m + 1] <= cv * 32) m++;
         const int limit = seg[m] + (overflow ? (cnt[m] & ~31) : cnt[m]);
         if (p < limit) {
             const int l = perm[p];
-            mine += lookup_and_store<GRID, ARITH, CHECKED>(t, sE[l], m, base + l, a.out_macro,
-                                                           a.out_idx, a.err);
+            mine += lookup_and_store<GRID, ARITH, CHECKED, TABLE>(t, sE[l], m, base + l, a.out_macro,
+                                                                  a.out_idx, a.err);
         }
     }
     block_verification(mine, &s_acc, a.verif);
@@ -217,8 +273,8 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
 // Persistent lookup over a material-segmented list (ListArgs).  Warps pull
 // 32-entry chunks from a global queue; fuel (material 0) comes first, so the
 // longest chunks start first.  No waits: a warp reads the queue once per chunk.
-template <int GRID, int ARITH, bool CHECKED>
-__global__ void __launch_bounds__(kBlock) k_list_lookup(Tables t, ListArgs a)
+template <int GRID, int ARITH, bool CHECKED, bool TABLE>
+__device__ __forceinline__ void list_lookup_body(const Tables &t, const ListArgs &a)
 {
     __shared__ int seg[kMaterials + 1], cnt[kMaterials], bas[kMaterials];
     __shared__ unsigned long long s_acc;
@@ -230,24 +286,53 @@ __global__ void __launch_bounds__(kBlock) k_list_lookup(Tables t, ListArgs a)
     }
     if (tid == 0) s_acc = 0;
     __syncthreads();
-    const int nchunks = seg[kMaterials] >> 5;
     const int lane = tid & 31;
+    // fuel chunks of 32 / L entries first (the fuel segment is [seg[0], seg[1])),
+    // then 32-entry chunks of the rest
+    const int L = (ARITH == XS_ARITH_FAST) ? a.fuel_lanes : 1;
+    const int nfuel = L > 1 ? (seg[1] - seg[0]) / (32 / L) : 0;
+    const int skip = L > 1 ? (seg[1] >> 5) : 0;
+    const int nchunks = nfuel + (seg[kMaterials] >> 5) - skip;
     unsigned long long mine = 0;
     for (;;) {
         unsigned int c = 0;
         if (lane == 0) c = atomicAdd(a.queue, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
         if ((int)c >= nchunks) break;
-        const int pv = (int)c * 32 + lane;
+        if (ARITH == XS_ARITH_FAST && (int)c < nfuel) {
+            const int q = lane & (L - 1);
+            const int pv = seg[0] + (int)c * (32 / L) + lane / L;
+            const bool live = pv < seg[0] + cnt[0];
+            const long p = live ? (long)bas[0] + (pv - seg[0]) : 0;
+            mine += split_lookup_and_store<GRID, CHECKED, TABLE>(t, live, live ? a.E[p] : 0.0,
+                                                                 live ? a.id[p] : 0, q, L,
+                                                                 a.out_macro, a.out_idx, a.err);
+            continue;
+        }
+        const int cv = (int)c - nfuel + skip;
+        const int pv = cv * 32 + lane;
         int m = 0;
-        while (seg[m + 1] <= (int)c * 32) m++;
+        while (seg[m + 1] <= cv * 32) m++;
         if (pv < seg[m] + cnt[m]) {
             const long p = (long)bas[m] + (pv - seg[m]);
-            mine += lookup_and_store<GRID, ARITH, CHECKED>(t, a.E[p], m, a.id[p], a.out_macro,
-                                                           a.out_idx, a.err);
+            mine += lookup_and_store<GRID, ARITH, CHECKED, TABLE>(t, a.E[p], m, a.id[p], a.out_macro,
+                                                                  a.out_idx, a.err);
         }
     }
     block_verification(mine, &s_acc, a.verif);
+}
+
+template <int GRID, int ARITH, bool CHECKED>
+__global__ void __launch_bounds__(kBlock) k_list_lookup(Tables t, ListArgs a)
+{
+    list_lookup_body<GRID, ARITH, CHECKED, false>(t, a);
+}
+
+// The union-table variant (FAST): more registers for loads in flight.
+template <int GRID>
+__global__ void __launch_bounds__(kBlock, 2) k_list_lookup_table(Tables t, ListArgs a)
+{
+    list_lookup_body<GRID, XS_ARITH_FAST, false, true>(t, a);
 }
 
 // ------------------------------------------------------- adjoint, energy ---
@@ -379,6 +464,12 @@ struct GridLaunch {
     } while (0)
         if (checked) XSGB_LIST(XS_ARITH_FAST, true);
         if (arith == XS_ARITH_EXACT) XSGB_LIST(XS_ARITH_EXACT, false);
+        if constexpr (GRID == XS_UNIONIZED) {
+            if (a.table && t.utab[0] != nullptr) {
+                k_list_lookup_table<GRID><<<blocks, kBlock, 0, st>>>(t, a);
+                return cudaGetLastError();
+            }
+        }
         XSGB_LIST(XS_ARITH_FAST, false);
 #undef XSGB_LIST
     }

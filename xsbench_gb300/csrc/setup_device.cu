@@ -339,6 +339,7 @@ extern "C" xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
         ctx->own_index = t.index_grid;
         s = build_derived_tables(ctx);
+        if (s == XS_OK) s = build_union_table(ctx);
     } while (0);
     if (s == XS_OK && e != cudaSuccess) s = cuda_fail(e, "device setup");
     cudaStreamSynchronize(st);

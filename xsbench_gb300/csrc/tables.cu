@@ -8,6 +8,13 @@
 //   coarse      every 16th key of each nuclide (NUCLIDE search, first level)
 //   union_keys  order keys of the unionized energies
 //   union_bins  for b = 0..2^L: #{union energies < b / 2^L}
+//   union table per material m and union row e, one 80-byte entry per
+//               nuclide j of m: the five pairs (v, s), v = the channel of
+//               nuclide j's interval line at u_e, s its slope; stored [e][j][c]
+//               (the unionized grid with every nuclide's cross sections
+//               reconstructed on it)
+#include <cstdlib>
+
 #include "device_common.cuh"
 
 namespace xsgb {
@@ -87,6 +94,63 @@ static unsigned grid_for(long n, int sm)
     long cap = (long)sm * 32;
     if (b > cap) b = cap;
     return (unsigned)(b < 1 ? 1 : b);
+}
+
+// Entry (e, j) of material m's union table.  The interval is the one the
+// reference's unionized lookup reads for (u_e, nuclide) (Simulation.c:264-272):
+// index_grid[e][nuc], moved down one at the top gridpoint.
+__global__ void k_union_table(Tables t, int m, int n_m, double2 *out)
+{
+    const long total = t.n_union * n_m;
+    const long top = t.n_gp - 1;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long)gridDim.x * blockDim.x) {
+        const long e = i / n_m;
+        const int j = (int)(i - e * n_m);
+        const int nuc = t.mats[m * t.max_nucs + j];
+        long k = t.index_grid[e * t.n_iso + nuc];
+        if (k == top) k -= 1;
+        const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * 6);
+        const double d = t.union_e[e] - r[0];
+        double2 *o = out + i * 5;
+#pragma unroll
+        for (int c = 0; c < 5; c++) o[c] = make_double2(fma(r[6 + c], d, r[1 + c]), r[6 + c]);
+    }
+}
+
+xs_status build_union_table(xs_ctx *ctx)
+{
+    Tables &t = ctx->t;
+    for (int m = 0; m < kMaterials; m++) t.utab[m] = nullptr;
+    ctx->union_table_bytes = 0;
+    if (t.grid_type != XS_UNIONIZED) return XS_OK;
+    if (const char *env = getenv("XSGB_UNION_TABLE"))
+        if (atoi(env) == 0) return XS_OK;
+    size_t need = 0;
+    for (int m = 0; m < kMaterials; m++) need += (size_t)t.n_union * ctx->num_nucs_host[m] * 80 + 256;
+    // built only when it leaves room for the runs' own buffers
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return XS_OK;
+    }
+    const size_t reserve = (size_t)24 << 30;
+    if (free_b < need + reserve) return XS_OK;
+    const int sm = ctx->sm_count;
+    for (int m = 0; m < kMaterials; m++) {
+        const int n_m = ctx->num_nucs_host[m];
+        if (n_m == 0) continue;
+        void *p = nullptr;
+        xs_status s = ctx_alloc(ctx, &p, (size_t)t.n_union * n_m * 80);
+        if (s != XS_OK) return s;
+        k_union_table<<<(unsigned)sm * 16, 256, 0, ctx->stream>>>(t, m, n_m, (double2 *)p);
+        XS_CUDA(cudaGetLastError());
+        t.utab[m] = (const double2 *)p;
+    }
+    XS_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->union_table_bytes = need;
+    if (!getenv("XSGB_BATCHED_FUEL_LANES")) ctx->batched_fuel_lanes = ctx->num_nucs_host[0] >= 64 ? 2 : 1;
+    return XS_OK;
 }
 
 xs_status build_derived_tables(xs_ctx *ctx)

@@ -50,6 +50,10 @@ struct Tables {
     int pair_base[kMaterials + 1];   // running sum of num_nucs: (material, position) pairs
     const int *inv_off;              // [n_iso + 1] pairs holding each nuclide (CSR)
     const int *inv_pair;             // [pairs] m * max_nucs + j, by nuclide, m ascending
+    // union table (UNIONIZED, FAST): per material m, [n_union][num_nucs[m]]
+    // entries of five (v, s) pairs: v = the nuclide's xs at the row's union
+    // energy, s = the slope of its interval there; null when not built
+    const double2 *utab[kMaterials];
 };
 
 // Per-run scratch in device memory (owned by the context).
@@ -88,6 +92,10 @@ struct xs_ctx {
     int plain_tile = 1024;
     int batched_buckets = 4096;
     int batched_blocks_per_sm = 4;
+    int fuel_lanes = 1;                       // plain kernel, FAST: lanes per fuel lookup
+    int batched_fuel_lanes = 1;               // the same for the batched kernel
+    int num_nucs_host[xsgb::kMaterials] = {}; // host copy of num_nucs
+    size_t union_table_bytes = 0;             // 0: no union table
     std::map<std::string, xsgb::BatchedGraph> graphs;
     int sm_count = 0;
     void *h_result = nullptr;                 // pinned: verification + error words
@@ -123,6 +131,8 @@ xs_status ctx_alloc(xs_ctx *ctx, void **p, size_t bytes);
 
 // derived-table builders (tables.cu)
 xs_status build_derived_tables(xs_ctx *ctx);
+// the union table, when the grid is unionized and device memory allows
+xs_status build_union_table(xs_ctx *ctx);
 
 // lookup launchers (lookup.cu).  Every launcher only enqueues on `st`.
 struct Outputs {
