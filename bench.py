@@ -393,7 +393,8 @@ def main():
         peak, peak_kind = measured_peak_gbs()
         per_launch_s = t / args.steps
         achieved = N * bpl / per_launch_s / 1e9
-        traffic_pl, traffic_src = profiled_traffic(args.workload, args.kernel)
+        traffic_pl, traffic_src = (None, None) if args.gridpoints else \
+            profiled_traffic(args.workload, args.kernel)
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             cpu = cpu_baseline_oracle(inputs, problem, args.workload, args.cpu_budget)

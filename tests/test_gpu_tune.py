@@ -31,6 +31,7 @@ def test_autotune_keeps_results_and_caches(tmp_path, name):
         (key, val), = entries.items()
         assert "GB300" in key or "|grid=" in key
         assert val["lookups_per_s"] > 0
+        assert val["fuel_lanes"] in (1, 2, 4)
         with X.Context(inp, p) as ctx2:
             t0 = time.perf_counter()
             best2 = ctx2.autotune(cache)

@@ -384,12 +384,14 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
             if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamSynchronize");
         }
     }
-    // a fuel list this long is split over 4 lanes per lookup in the plain
-    // kernel (FAST arithmetic) and over 2 in the batched kernel when it reads
-    // the union table (set by build_union_table); XSGB_FUEL_LANES and
-    // XSGB_BATCHED_FUEL_LANES = 1, 2 or 4 override
+    // a long fuel list is split over 4 lanes per lookup in the plain kernel
+    // (FAST arithmetic) and over 2 in the batched kernel when it reads the
+    // union table (set by build_union_table); xs_autotune measures 1, 2 and 4;
+    // XSGB_FUEL_LANES and XSGB_BATCHED_FUEL_LANES = 1, 2 or 4 override
     for (int m = 0; m < kMaterials; m++) ctx->num_nucs_host[m] = sd->num_nucs[m];
-    ctx->fuel_lanes = sd->num_nucs[0] >= 64 ? 4 : 1;
+    // (measured: 4 lanes win up to ~11,000 gridpoints per nuclide and lose on
+    // the 238,847-point XL grid)
+    ctx->fuel_lanes = (sd->num_nucs[0] >= 64 && in->n_gridpoints <= 65536) ? 4 : 1;
     if (const char *env = getenv("XSGB_FUEL_LANES")) {
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->fuel_lanes = v;

@@ -83,7 +83,7 @@ static std::string cache_key(const xs_ctx *ctx)
 }
 
 struct Choice {
-    int grid_type = -1, kernel = 0, tile = 1024, buckets = 4096, blocks_per_sm = 4;
+    int grid_type = -1, kernel = 0, tile = 1024, buckets = 4096, blocks_per_sm = 4, lanes = 1;
     double rate = 0;
 };
 
@@ -100,8 +100,10 @@ static bool cache_read(const char *path, const std::string &key, Choice &c)
         if (!p) continue;
         p += want.size();
         if (sscanf(p, " {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
-                      "\"blocks_per_sm\": %d, \"lookups_per_s\": %lf",
-                   &c.grid_type, &c.kernel, &c.tile, &c.buckets, &c.blocks_per_sm, &c.rate) == 6)
+                      "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"lookups_per_s\": %lf",
+                   &c.grid_type, &c.kernel, &c.tile, &c.buckets, &c.blocks_per_sm, &c.lanes,
+                   &c.rate) == 7 &&
+            (c.lanes == 1 || c.lanes == 2 || c.lanes == 4))
             found = true;
     }
     fclose(f);
@@ -126,8 +128,9 @@ static void cache_write(const char *path, const std::string &key, const Choice &
     char buf[1024];
     snprintf(buf, sizeof buf,
              "  \"%s\": {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
-             "\"blocks_per_sm\": %d, \"lookups_per_s\": %.6g}",
-             key.c_str(), c.grid_type, c.kernel, c.tile, c.buckets, c.blocks_per_sm, c.rate);
+             "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"lookups_per_s\": %.6g}",
+             key.c_str(), c.grid_type, c.kernel, c.tile, c.buckets, c.blocks_per_sm, c.lanes,
+             c.rate);
     lines.push_back(buf);
     FILE *f = fopen(path, "w");
     if (!f) return;
@@ -201,43 +204,51 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
             return XS_OK;
         };
         const int saved_bps = ctx->batched_blocks_per_sm;
+        const int saved_lanes = ctx->fuel_lanes, saved_blanes = ctx->batched_fuel_lanes;
+        auto restore = [&]() {
+            apply_view(t, original);
+            ctx->batched_blocks_per_sm = saved_bps;
+            ctx->fuel_lanes = saved_lanes;
+            ctx->batched_fuel_lanes = saved_blanes;
+        };
         for (const GridView &v : views) {
             apply_view(t, v);
             for (int bps : {3, 4}) {
                 ctx->batched_blocks_per_sm = bps;
-                for (int tile : {512, 1024, 2048}) {
-                    xs_run_opts o;
-                    xs_run_opts_init(&o);
-                    o.count = sample;
-                    o.tile_lookups = tile;
-                    double rate = 0;
-                    xs_status s = time_run(o, &rate);
-                    if (s != XS_OK) {
-                        apply_view(t, original);
-                        ctx->batched_blocks_per_sm = saved_bps;
-                        return s;
+                for (int lanes : {1, 2, 4}) {
+                    ctx->fuel_lanes = lanes;
+                    ctx->batched_fuel_lanes = lanes;
+                    for (int tile : {512, 1024, 2048}) {
+                        xs_run_opts o;
+                        xs_run_opts_init(&o);
+                        o.count = sample;
+                        o.tile_lookups = tile;
+                        double rate = 0;
+                        xs_status s = time_run(o, &rate);
+                        if (s != XS_OK) {
+                            restore();
+                            return s;
+                        }
+                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, lanes, rate};
                     }
-                    if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, rate};
-                }
-                for (int nb : {256, 1024, 4096, 16384}) {
-                    xs_run_opts o;
-                    xs_run_opts_init(&o);
-                    o.count = sample;
-                    o.kernel = XS_KERNEL_BATCHED;
-                    o.energy_buckets = nb;
-                    double rate = 0;
-                    xs_status s = time_run(o, &rate);
-                    if (s != XS_OK) {
-                        apply_view(t, original);
-                        ctx->batched_blocks_per_sm = saved_bps;
-                        return s;
+                    for (int nb : {256, 1024, 4096, 16384}) {
+                        xs_run_opts o;
+                        xs_run_opts_init(&o);
+                        o.count = sample;
+                        o.kernel = XS_KERNEL_BATCHED;
+                        o.energy_buckets = nb;
+                        double rate = 0;
+                        xs_status s = time_run(o, &rate);
+                        if (s != XS_OK) {
+                            restore();
+                            return s;
+                        }
+                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, lanes, rate};
                     }
-                    if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, rate};
                 }
             }
         }
-        apply_view(t, original);
-        ctx->batched_blocks_per_sm = saved_bps;
+        restore();
         if (cache_path) cache_write(cache_path, key, c);
     }
     // install the choice
@@ -246,6 +257,10 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
     ctx->plain_tile = c.tile;
     ctx->batched_buckets = c.buckets;
     ctx->batched_blocks_per_sm = c.blocks_per_sm;
+    if (c.kernel == XS_KERNEL_PLAIN)
+        ctx->fuel_lanes = c.lanes;
+    else
+        ctx->batched_fuel_lanes = c.lanes;
     for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
     ctx->graphs.clear();
     if (best) {
