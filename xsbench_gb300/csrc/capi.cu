@@ -356,6 +356,8 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
             if (v >= 0.0 && v <= 1.0) frac = v;
         }
         const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = (size_t)(l2 * frac);
+        t.cold_normal = 0;
+        if (const char *env = getenv("XSGB_L2_COLD")) t.cold_normal = strcmp(env, "normal") == 0;
         size_t used = 0;
         std::memset(t.hot, 0, sizeof t.hot);
         for (int n : order) {

@@ -212,13 +212,34 @@ __device__ __forceinline__ unsigned long long policy_first()
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+__device__ __forceinline__ unsigned long long policy_normal()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
 __device__ __forceinline__ bool is_hot(const Tables &t, int nuc)
 {
     return nuc < 512 && ((t.hot[nuc >> 5] >> (nuc & 31)) & 1u);
 }
 __device__ __forceinline__ unsigned long long record_policy(const Tables &t, int nuc)
 {
-    return is_hot(t, nuc) ? policy_last() : policy_first();
+    return is_hot(t, nuc) ? policy_last() : (t.cold_normal ? policy_normal() : policy_first());
+}
+#ifndef XSGB_PREFETCH_POL
+#define XSGB_PREFETCH_POL 2
+#endif
+// Policy of the L2 prefetch of a record that the lane reads a nuclide later:
+// evict_last, so the line survives until that load, which reads it with
+// record_policy (evict_first for the cold records) and so releases it.
+// 0: record_policy, 1: evict_normal, 2: evict_last (default; 2.5 % fewer
+// DRAM bytes than 0).
+__device__ __forceinline__ unsigned long long prefetch_policy(const Tables &t, int nuc)
+{
+    if (is_hot(t, nuc)) return policy_last();
+    if (XSGB_PREFETCH_POL == 1) return policy_normal();
+    if (XSGB_PREFETCH_POL == 2) return policy_last();
+    return t.cold_normal ? policy_normal() : policy_first();
 }
 
 // ------------------------------------------------------------- prefetch ---
@@ -322,6 +343,10 @@ __device__ __forceinline__ const void *interval_bytes(const Tables &t, int nuc, 
     return t.records + ((long)nuc * (t.n_gp - 1) + k) * 6;
 }
 
+#ifndef XSGB_PIPE_P
+#define XSGB_PIPE_P 1   // records prefetched this many nuclides ahead (unionized loop);
+#endif                  // 2 and 3 measured 4 % and 14 % slower (records evicted before use)
+
 // UNIONIZED nuclide loop, software-pipelined: the index entry of nuclide j+2P
 // is loaded and the 96-byte interval of nuclide j+P is prefetched into L2 while
 // nuclide j is interpolated, so a lane keeps three gathers in flight instead
@@ -359,7 +384,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
         }
         return;
     }
-    constexpr int P = 2;
+    constexpr int P = XSGB_PIPE_P;
     const int *irow = t.index_grid + row * t.n_iso;
     if (q0 == 0) {
         // the material's span of the index row, 16-byte aligned
@@ -381,7 +406,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             long k = kr[q];
             if (CHECKED && (k < 0 || k > top)) k = 0;
             const int nq = ldg(&mrow[q * stride]);
-            prefetch_l2(interval_bytes<ARITH>(t, nq, k == top ? k - 1 : k), 96, record_policy(t, nq));
+            prefetch_l2(interval_bytes<ARITH>(t, nq, k == top ? k - 1 : k), 96, prefetch_policy(t, nq));
         }
     for (int j0 = 0; j0 < nl; j0 += 2 * P) {
 #pragma unroll
@@ -402,7 +427,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
                     if (CHECKED && (kp < 0 || kp > top)) kp = 0;
                     const int np = ldg(&mrow[jp * stride]);
                     prefetch_l2(interval_bytes<ARITH>(t, np, kp == top ? kp - 1 : kp), 96,
-                                record_policy(t, np));
+                                prefetch_policy(t, np));
                 }
                 const int nuc = ldg(&mrow[j * stride]);
                 const double conc = ldg(&crow[j * stride]);
