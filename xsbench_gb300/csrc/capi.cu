@@ -582,11 +582,22 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
                                const int *mat, long n, double *macro_out, unsigned char *idx_out,
                                xs_run_result *result)
 {
-    const long chunk = o.tile_lookups > 0 && o.kernel == XS_KERNEL_PLAIN ? std::max<long>(1L << 20, o.tile_lookups) : (1L << 21);
+    long chunk = o.tile_lookups > 0 && o.kernel == XS_KERNEL_PLAIN ? std::max<long>(1L << 20, o.tile_lookups) : (1L << 21);
+    if (const char *env = getenv("XSGB_PIPE_CHUNK")) {
+        const long v = atol(env);
+        if (v >= 4096 && v <= (1L << 26)) chunk = std::max<long>(v, o.tile_lookups);
+    }
     const size_t per = 8 + 4 + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
     const size_t io_bytes = ((size_t)chunk * per + 1023) & ~(size_t)255;
     const bool ovf = o.kernel == XS_KERNEL_PLAIN && use_overflow(ctx, chunk, o.tile_lookups);
-    const size_t slot = io_bytes + (ovf ? plain_scratch_bytes(chunk, o.tile_lookups) : 0);
+    // batched: each stream has its own sort buffers, so the two streams overlap
+    const bool batched = o.kernel == XS_KERNEL_BATCHED;
+    int nb_log2 = 0;
+    while ((1 << nb_log2) < o.energy_buckets) nb_log2++;
+    if (batched && ((1 << nb_log2) != o.energy_buckets || o.energy_buckets > 65536))
+        return fail(XS_ERR_INVALID_ARGUMENT, "energy_buckets %d must be a power of two <= 65536", o.energy_buckets);
+    const size_t slot = io_bytes + (ovf ? plain_scratch_bytes(chunk, o.tile_lookups) : 0) +
+                        (batched ? ((batched_scratch_bytes(chunk, o.energy_buckets) + 255) & ~(size_t)255) : 0);
     const size_t need = 2 * slot;
     if (ctx->pipe_bytes < need) {
         if (ctx->pipe_buf) {
@@ -634,16 +645,15 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
             if (ovf) ps = carve_plain_scratch(b + io_bytes, chunk, o.tile_lookups);
             s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, in, out,
                              ovf && use_overflow(ctx, m, o.tile_lookups) ? &ps : nullptr, &launches);
-        } else
-            s = launch_batched(ctx, st, o.arith, o.checked, 0, m, 256, o.energy_buckets, in, out, &launches);
+        } else {
+            BatchedScratch bs = carve_batched_scratch(b + io_bytes, chunk, nb_log2);
+            bs.verification = ctx->s.verification;
+            bs.error = ctx->s.error;
+            s = enqueue_batched_buf(ctx, st, o.arith, o.checked, 0, m, nb_log2, in, out, bs, &launches);
+        }
         if (s != XS_OK) return s;
         if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));
         if (idx_out) XS_CUDA(cudaMemcpyAsync(idx_out + c0, dIdx, (size_t)m, cudaMemcpyDeviceToHost, st));
-        if (o.kernel == XS_KERNEL_BATCHED) {
-            // the batched sort buffers are shared: serialise the two streams
-            XS_CUDA(cudaEventRecord(ctx->pipe_event[w], st));
-            XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[w ^ 1], ctx->pipe_event[w], 0));
-        }
     }
     for (int i = 0; i < 2; i++) {
         XS_CUDA(cudaEventRecord(ctx->pipe_event[i], ctx->pipe_stream[i]));

@@ -275,24 +275,35 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
 }
 
 // Enqueues the batched pipeline on `st` (used directly or under capture).
-static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                                 long count, int nb_log2, const SampleInput &in,
-                                 const Outputs &out, int *launches)
+BatchedScratch carve_batched_scratch(void *buf, long count, int nb_log2)
 {
     const int nb = 1 << nb_log2;
-    char *b = (char *)ctx->s.sort_buf;
-    int *offs = (int *)b;
+    char *b = (char *)buf;
+    BatchedScratch r;
+    r.offs = (int *)b;
     size_t off = ((size_t)kMaterials * nb * 4 + 255) & ~(size_t)255;
-    int *seg = (int *)(b + off);
-    int *cnt = seg + 16;
+    r.seg = (int *)(b + off);         // [13]
+    r.cnt = r.seg + 16;               // [12]
+    r.queue = (unsigned int *)(r.seg + 32);
     off += 256;
-    double *sE = (double *)(b + off);
+    r.sE = (double *)(b + off);
     off += ((size_t)count + kMaterials * 32) * 8;
     off = (off + 255) & ~(size_t)255;
-    int *sid = (int *)(b + off);
+    r.sid = (int *)(b + off);
+    r.verification = nullptr;
+    r.error = nullptr;
+    return r;
+}
 
-    XS_CUDA(cudaMemsetAsync(offs, 0, (size_t)kMaterials * nb * 4, st));
-    XS_CUDA(cudaMemsetAsync(ctx->s.queue, 0, sizeof(unsigned int), st));
+// The batched run on explicit buffers (b.verification / b.error set): clears
+// the bucket offsets and the queue, sorts, runs the lookups.  Four launches.
+xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                              long count, int nb_log2, const SampleInput &in, const Outputs &out,
+                              const BatchedScratch &b, int *launches)
+{
+    const int nb = 1 << nb_log2;
+    XS_CUDA(cudaMemsetAsync(b.offs, 0, (size_t)kMaterials * nb * 4, st));
+    XS_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(unsigned int), st));
     const bool samples = in.energy != nullptr;
     unsigned blocks;
     if (samples) {
@@ -300,36 +311,47 @@ static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int ch
         long cap = (long)ctx->sm_count * 8;
         blocks = (unsigned)(want < cap ? want : cap);
         if (blocks == 0) blocks = 1;
-        k_sort_pass<true, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+        k_sort_pass<true, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, b.offs, b.sE, b.sid, b.error);
     } else {
         blocks = (unsigned)((count + (long)kBlock * kSortLpt - 1) / ((long)kBlock * kSortLpt));
-        k_sort_pass<false, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+        k_sort_pass<false, false><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, b.offs, b.sE, b.sid, b.error);
     }
     XS_CUDA(cudaGetLastError());
-    k_sort_scan<<<1, kScanThreads, 0, st>>>(offs, nb_log2, seg, cnt);
+    k_sort_scan<<<1, kScanThreads, 0, st>>>(b.offs, nb_log2, b.seg, b.cnt);
     XS_CUDA(cudaGetLastError());
     if (samples)
-        k_sort_pass<true, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, offs, sE, sid, ctx->s.error);
+        k_sort_pass<true, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, in.energy, in.mat, b.offs, b.sE, b.sid, b.error);
     else
-        k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, offs, sE, sid, ctx->s.error);
+        k_sort_pass<false, true><<<blocks, kBlock, 0, st>>>(ctx->t, first, count, nb_log2, nullptr, nullptr, b.offs, b.sE, b.sid, b.error);
     XS_CUDA(cudaGetLastError());
     ListArgs l;
-    l.seg_v = seg;
-    l.cnt = cnt;
+    l.seg_v = b.seg;
+    l.cnt = b.cnt;
     l.base = nullptr;
-    l.E = sE;
-    l.id = sid;
-    l.queue = ctx->s.queue;
+    l.E = b.sE;
+    l.id = b.sid;
+    l.queue = b.queue;
     l.out_macro = out.macro;
     l.out_idx = out.max_idx;
-    l.verif = ctx->s.verification;
-    l.err = ctx->s.error;
+    l.verif = b.verification;
+    l.err = b.error;
     l.fuel_lanes = ctx->batched_fuel_lanes;
     l.table = 1;
     XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
                                       ctx->sm_count * ctx->batched_blocks_per_sm, l));
     if (launches) *launches += 4;
     return XS_OK;
+}
+
+static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                                 long count, int nb_log2, const SampleInput &in,
+                                 const Outputs &out, int *launches)
+{
+    BatchedScratch b = carve_batched_scratch(ctx->s.sort_buf, count, nb_log2);
+    b.queue = ctx->s.queue;
+    b.verification = ctx->s.verification;
+    b.error = ctx->s.error;
+    return enqueue_batched_buf(ctx, st, arith, checked, first, count, nb_log2, in, out, b, launches);
 }
 
 // The (material, energy-bucket) counting sort alone, for the adjoint: fills

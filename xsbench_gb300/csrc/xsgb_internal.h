@@ -179,6 +179,12 @@ struct BatchedScratch {
 };
 xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
                              int nb_log2, const BatchedScratch &b, const Outputs &out);
+// Buffers of one batched run carved from `buf` (batched_scratch_bytes(count,
+// 1 << nb_log2) bytes); verification and error are left null for the caller.
+BatchedScratch carve_batched_scratch(void *buf, long count, int nb_log2);
+xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                              long count, int nb_log2, const SampleInput &in, const Outputs &out,
+                              const BatchedScratch &b, int *launches);
 xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat);
 
 struct ListArgs;
