@@ -129,69 +129,168 @@ __global__ void k_gather_gbar(const int *seg, const int *cnt, const int *sid, co
 
 // ------------------------------------------------------- prefix of gbar ---
 // EP[p] = sum_{q < p} sg[q] per channel, over all P positions (padding holds
-// zeros), by a three-phase scan with a fixed shape: block sums, one-block scan
-// of the block sums, block-local scan plus offset.
-constexpr int kScanBlock = 1024;
+// zeros), by a three-phase scan with a fixed shape (the same additions in the
+// same order on every run): tile sums, a one-block scan of the tile sums, a
+// tile-local scan plus the tile's offset.  A tile is 1,024 positions x 5
+// channels, staged through shared memory so that every global access is
+// coalesced; each of the 256 threads owns 4 consecutive positions.
+constexpr int kScanBlock = 1024;               // positions per tile
+constexpr int kScanThreads2 = 256;
+constexpr int kScanPer = kScanBlock / kScanThreads2;
 
-__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(const int *seg, const double *sg,
-                                                            double *bsum)
+// the tile's 5120 doubles into shared memory (zeros past `total`)
+__device__ __forceinline__ void scan_stage(const double *sg, long tile0, int total, double *sh)
 {
-    __shared__ double red[kScanBlock];
+    const long base = tile0 * 5;
+    const long end = (long)total * 5;
+    for (int i = threadIdx.x; i < kScanBlock * 5; i += kScanThreads2)
+        sh[i] = base + i < end ? sg[base + i] : 0.0;
+}
+
+// inclusive scan of v over the warp's lanes (fixed shape)
+__device__ __forceinline__ double warp_incl(double v, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(kScanThreads2) k_scan_blocks(const int *seg, const double *sg,
+                                                               double *bsum)
+{
+    __shared__ double sh[kScanBlock * 5];
+    __shared__ double wsum[kScanThreads2 / 32][5];
     const int total = seg[kMaterials];
     const int nblocks = (total + kScanBlock - 1) / kScanBlock;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        for (int c = 0; c < 5; c++) {
-            const long p = (long)b * kScanBlock + threadIdx.x;
-            red[threadIdx.x] = p < total ? sg[p * 5 + c] : 0.0;
-            __syncthreads();
-            for (int w = kScanBlock / 2; w > 0; w >>= 1) {
-                if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) bsum[(long)b * 5 + c] = red[0];
-            __syncthreads();
+        scan_stage(sg, (long)b * kScanBlock, total, sh);
+        __syncthreads();
+        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < kScanPer; i++) {
+            const double *x = sh + (threadIdx.x * kScanPer + i) * 5;
+#pragma unroll
+            for (int c = 0; c < 5; c++) v[c] += x[c];
         }
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            const double w = warp_incl(v[c], lane);
+            if (lane == 31) wsum[warp][c] = w;
+        }
+        __syncthreads();
+        if (threadIdx.x < 5) {
+            double t = 0.0;
+            for (int w = 0; w < kScanThreads2 / 32; w++) t += wsum[w][threadIdx.x];
+            bsum[(long)b * 5 + threadIdx.x] = t;
+        }
+        __syncthreads();
     }
 }
 
-// exclusive scan of the block sums, sequentially in block order (one thread
-// per channel)
-__global__ void k_scan_bsums(const int *seg, double *bsum)
+// exclusive scan of the tile sums in one block: each thread a contiguous run
+// of tiles, then a scan of the threads' totals
+__global__ void __launch_bounds__(1024) k_scan_bsums(const int *seg, double *bsum)
 {
-    const int c = threadIdx.x;
-    if (c >= 5) return;
+    __shared__ double wtot[32][5];
     const int nblocks = (seg[kMaterials] + kScanBlock - 1) / kScanBlock;
-    double run = 0.0;
-    for (int b = 0; b < nblocks; b++) {
-        const double v = bsum[(long)b * 5 + c];
-        bsum[(long)b * 5 + c] = run;
-        run += v;
+    const int per = (nblocks + 1023) / 1024;
+    const int a = threadIdx.x * per, e = min(nblocks, a + per);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = a; b < e; b++)
+#pragma unroll
+        for (int c = 0; c < 5; c++) tot[c] += bsum[(long)b * 5 + c];
+    double incl[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        incl[c] = warp_incl(tot[c], lane);
+        if (lane == 31) wtot[warp][c] = incl[c];
     }
+    __syncthreads();
+    if (threadIdx.x < 5) {   // exclusive scan of the 32 warp totals, in order
+        double run = 0.0;
+        for (int w = 0; w < 32; w++) {
+            const double v = wtot[w][threadIdx.x];
+            wtot[w][threadIdx.x] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    double run[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) run[c] = wtot[warp][c] + (incl[c] - tot[c]);
+    for (int b = a; b < e; b++)
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            const double v = bsum[(long)b * 5 + c];
+            bsum[(long)b * 5 + c] = run[c];
+            run[c] += v;
+        }
 }
 
-__global__ void __launch_bounds__(kScanBlock) k_scan_local(const int *seg, const double *sg,
-                                                           const double *bsum, double *ep)
+__global__ void __launch_bounds__(kScanThreads2) k_scan_local(const int *seg, const double *sg,
+                                                              const double *bsum, double *ep)
 {
-    __shared__ double buf[kScanBlock];
+    __shared__ double sh[kScanBlock * 5];
+    __shared__ double woff[kScanThreads2 / 32][5];
     const int total = seg[kMaterials];
     const int nblocks = (total + kScanBlock - 1) / kScanBlock;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        for (int c = 0; c < 5; c++) {
-            const long p = (long)b * kScanBlock + threadIdx.x;
-            buf[threadIdx.x] = p < total ? sg[p * 5 + c] : 0.0;
-            __syncthreads();
-            // Hillis-Steele inclusive scan (fixed shape)
-            for (int o = 1; o < kScanBlock; o <<= 1) {
-                const double v = threadIdx.x >= o ? buf[threadIdx.x - o] : 0.0;
-                __syncthreads();
-                buf[threadIdx.x] += v;
-                __syncthreads();
-            }
-            const double excl = (threadIdx.x ? buf[threadIdx.x - 1] : 0.0);
-            if (p < total) ep[p * 5 + c] = bsum[(long)b * 5 + c] + excl;
-            if (p == total - 1) ep[(long)total * 5 + c] = bsum[(long)b * 5 + c] + buf[threadIdx.x];
-            __syncthreads();
+        const long tile0 = (long)b * kScanBlock;
+        scan_stage(sg, tile0, total, sh);
+        __syncthreads();
+        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int i = 0; i < kScanPer; i++) {
+            const double *x = sh + (threadIdx.x * kScanPer + i) * 5;
+#pragma unroll
+            for (int c = 0; c < 5; c++) v[c] += x[c];
         }
+        double incl[5];
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            incl[c] = warp_incl(v[c], lane);
+            if (lane == 31) woff[warp][c] = incl[c];
+        }
+        __syncthreads();
+        if (threadIdx.x < 5) {   // exclusive offsets of the 8 warps, plus the tile's
+            double run = bsum[(long)b * 5 + threadIdx.x];
+            for (int w = 0; w < kScanThreads2 / 32; w++) {
+                const double t = woff[w][threadIdx.x];
+                woff[w][threadIdx.x] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        double run[5];
+#pragma unroll
+        for (int c = 0; c < 5; c++) run[c] = woff[warp][c] + (incl[c] - v[c]);
+        // exclusive prefix of each of the thread's positions, in place
+        for (int i = 0; i < kScanPer; i++) {
+            double *x = sh + (threadIdx.x * kScanPer + i) * 5;
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                const double t = x[c];
+                x[c] = run[c];
+                run[c] += t;
+            }
+        }
+        // the prefix after the last position
+        const int last = total - 1 - (int)tile0;
+        if (last >= 0 && last / kScanPer == (int)threadIdx.x) {
+            // run[] now holds the inclusive prefix of this thread's last position;
+            // past the end of the data the staged zeros kept it unchanged
+#pragma unroll
+            for (int c = 0; c < 5; c++) ep[(long)total * 5 + c] = run[c];
+        }
+        __syncthreads();
+        const long base = tile0 * 5, end = (long)total * 5;
+        for (int i = threadIdx.x; i < kScanBlock * 5; i += kScanThreads2)
+            if (base + i < end) ep[base + i] = sh[i];
+        __syncthreads();
     }
 }
 
@@ -530,7 +629,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     l.verif = ctx->s.verification;
     l.err = ctx->s.error;
     l.fuel_lanes = 1;
-    l.table = 0;
+    l.table = 1;   // the forward reads the union table when there is one
     s = launch_adjoint_energy(ctx, st, l, sg, d_energy);
     if (s != XS_OK) return s;
 
@@ -540,9 +639,9 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
         XS_CUDA(cudaMemsetAsync(queue + 4, 0, 4, st));
         k_adj_layout<<<1, 32, 0, st>>>(t, cnt, L);
         XS_CUDA(cudaGetLastError());
-        k_scan_blocks<<<ctx->sm_count * 2, kScanBlock, 0, st>>>(seg, sg, bsum);
-        k_scan_bsums<<<1, 32, 0, st>>>(seg, bsum);
-        k_scan_local<<<ctx->sm_count * 2, kScanBlock, 0, st>>>(seg, sg, bsum, ep);
+        k_scan_blocks<<<ctx->sm_count * 4, kScanThreads2, 0, st>>>(seg, sg, bsum);
+        k_scan_bsums<<<1, 1024, 0, st>>>(seg, bsum);
+        k_scan_local<<<ctx->sm_count * 4, kScanThreads2, 0, st>>>(seg, sg, bsum, ep);
         XS_CUDA(cudaGetLastError());
         k_adj_transposed<<<ctx->sm_count * 4, 256, 0, st>>>(t, seg, cnt, sE, sg, ep, L, queue + 4, table, slots);
         XS_CUDA(cudaGetLastError());

@@ -381,6 +381,13 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             macro[2] = fma(fma(a2.y, dl, a2.x), conc, macro[2]);
             macro[3] = fma(fma(a3.y, dl, a3.x), conc, macro[3]);
             macro[4] = fma(fma(a4.y, dl, a4.x), conc, macro[4]);
+            if (DE) {  // d macro / dE = sum over nuclides of conc * slope
+                S[0] = fma(conc, a0.y, S[0]);
+                S[1] = fma(conc, a1.y, S[1]);
+                S[2] = fma(conc, a2.y, S[2]);
+                S[3] = fma(conc, a3.y, S[3]);
+                S[4] = fma(conc, a4.y, S[4]);
+            }
         }
         return;
     }

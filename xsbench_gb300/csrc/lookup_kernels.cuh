@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_list_lookup_table(Tables t, ListA
 // Over the adjoint's sorted list: the forward macro_xs (FAST arithmetic) and
 // dL/dE = sum_c gbar_c * sum_j conc_j * slope_jc, per lookup.  sg holds the
 // upstream gradients in sorted order (5 per position).
-template <int GRID>
+template <int GRID, bool TABLE = false>
 __global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, const double *sg,
                                                          double *d_energy)
 {
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, c
         if (p < seg[m] + cnt[m]) {
             const long id = a.id[p];
             double macro[5], S[5];
-            macro_xs<GRID, XS_ARITH_FAST, false, true>(t, a.E[p], m, macro, a.err, S);
+            macro_xs<GRID, XS_ARITH_FAST, false, true, TABLE>(t, a.E[p], m, macro, a.err, S);
             const int arg = argmax5(macro);
             mine += (unsigned)(arg + 1);
             if (a.out_macro) {
@@ -519,6 +519,12 @@ XSGB_DECLARE_GRID(hash)
     cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
                                const double *sg, double *d_energy)                              \
     {                                                                                           \
+        if constexpr (GRID == XS_UNIONIZED) {                                                   \
+            if (a.table && t.utab[0] != nullptr) {                                              \
+                k_list_adjoint<GRID, true><<<blocks, kBlock, 0, st>>>(t, a, sg, d_energy);      \
+                return cudaGetLastError();                                                      \
+            }                                                                                   \
+        }                                                                                       \
         k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, sg, d_energy);                    \
         return cudaGetLastError();                                                              \
     }
