@@ -16,11 +16,13 @@
 //      (energy, index) -- a deterministic total order per material;
 //   2. the upstream gradients gathered into that order;
 //   3. per lookup: forward macro_xs and dL/dE (interval search recomputed);
-//   4. transposed pass: a warp takes a chunk of one material's sorted lookups
-//      and lanes take that material's nuclides; each lane walks its nuclide's
-//      intervals alongside the rising energies and accumulates
-//      A_kc = sum g_ic (E_hi - E_i) and G_kc per interval; intervals inside the
-//      chunk are stored, the first and last go to per-chunk boundary slots;
+//   4. chunk-local prefixes of g and g (E - Eref) over each chunk of 2,048
+//      sorted lookups; transposed pass: lanes take a chunk's nuclides, and each
+//      lane walks its nuclide's intervals across the chunk, finding the end of
+//      each interval's run of lookups by a galloping search and taking
+//      G_kc = sum g_ic and A_kc = sum g_ic (E_hi - E_i) from the prefixes;
+//      intervals inside the chunk are stored, the first and last go to
+//      per-chunk boundary slots;
 //   5. boundary slots added into the interval table chunk by chunk, in order;
 //   6. dL/dxs per gridpoint (materials in order) and dL/dconcs per (m, j)
 //      (fixed-shape tree), added into the caller's arrays.
@@ -127,24 +129,38 @@ __global__ void k_gather_gbar(const int *seg, const int *cnt, const int *sid, co
     }
 }
 
-// ------------------------------------------------------- prefix of gbar ---
-// EP[p] = sum_{q < p} sg[q] per channel, over all P positions (padding holds
-// zeros), by a three-phase scan with a fixed shape (the same additions in the
-// same order on every run): tile sums, a one-block scan of the tile sums, a
-// tile-local scan plus the tile's offset.  A tile is 1,024 positions x 5
-// channels, staged through shared memory so that every global access is
-// coalesced; each of the 256 threads owns 4 consecutive positions.
-constexpr int kScanBlock = 1024;               // positions per tile
-constexpr int kScanThreads2 = 256;
-constexpr int kScanPer = kScanBlock / kScanThreads2;
+// ---------------------------------------------------- transposed layout ---
+struct AdjLayout {
+    int nchunks[kMaterials];
+    int group[kMaterials];     // lanes per chunk (power of two >= num_nucs, <= 32)
+    int task_off[kMaterials + 1];
+    long slot_base[kMaterials];
+    int chunk_off[kMaterials + 1];  // global number of each material's first chunk
+};
 
-// the tile's 5120 doubles into shared memory (zeros past `total`)
-__device__ __forceinline__ void scan_stage(const double *sg, long tile0, int total, double *sh)
+__global__ void k_adj_layout(Tables t, const int *cnt, AdjLayout *L)
 {
-    const long base = tile0 * 5;
-    const long end = (long)total * 5;
-    for (int i = threadIdx.x; i < kScanBlock * 5; i += kScanThreads2)
-        sh[i] = base + i < end ? sg[base + i] : 0.0;
+    if (threadIdx.x != 0) return;
+    int task = 0, chunks = 0;
+    long slot = 0;
+    for (int m = 0; m < kMaterials; m++) {
+        const int nn = t.num_nucs[m];
+        int G = 1;
+        while (G < nn && G < 32) G <<= 1;
+        const int ngroups = (nn + G - 1) / G;
+        const int S = 32 / G;
+        const int nch = (cnt[m] + kAdjChunk - 1) / kAdjChunk;
+        L->nchunks[m] = nch;
+        L->group[m] = G;
+        L->task_off[m] = task;
+        L->slot_base[m] = slot;
+        L->chunk_off[m] = chunks;
+        task += nn ? ngroups * ((nch + S - 1) / S) : 0;
+        slot += (long)nn * nch * 2;
+        chunks += nch;
+    }
+    L->task_off[kMaterials] = task;
+    L->chunk_off[kMaterials] = chunks;
 }
 
 // inclusive scan of v over the warp's lanes (fixed shape)
@@ -158,170 +174,80 @@ __device__ __forceinline__ double warp_incl(double v, int lane)
     return v;
 }
 
-__global__ void __launch_bounds__(kScanThreads2) k_scan_blocks(const int *seg, const double *sg,
-                                                               double *bsum)
-{
-    __shared__ double sh[kScanBlock * 5];
-    __shared__ double wsum[kScanThreads2 / 32][5];
-    const int total = seg[kMaterials];
-    const int nblocks = (total + kScanBlock - 1) / kScanBlock;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        scan_stage(sg, (long)b * kScanBlock, total, sh);
-        __syncthreads();
-        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int i = 0; i < kScanPer; i++) {
-            const double *x = sh + (threadIdx.x * kScanPer + i) * 5;
-#pragma unroll
-            for (int c = 0; c < 5; c++) v[c] += x[c];
-        }
-#pragma unroll
-        for (int c = 0; c < 5; c++) {
-            const double w = warp_incl(v[c], lane);
-            if (lane == 31) wsum[warp][c] = w;
-        }
-        __syncthreads();
-        if (threadIdx.x < 5) {
-            double t = 0.0;
-            for (int w = 0; w < kScanThreads2 / 32; w++) t += wsum[w][threadIdx.x];
-            bsum[(long)b * 5 + threadIdx.x] = t;
-        }
-        __syncthreads();
-    }
-}
+// ------------------------------------------------- chunk-local prefixes ---
+// For chunk (m, c) = sorted positions [a, b) with Eref = sE[a]: at entry
+// a + gc + (i - a), i in [a, b], the exclusive prefixes over [a, i) of
+//   g_c             (5 doubles)  and   g_c * (E - Eref)   (5 doubles),
+// gc being the chunk's global number (one extra entry per chunk).  Local
+// prefixes keep the terms and the differences taken from them small; one
+// block per chunk, 8 consecutive positions per thread, a fixed-shape scan.
+constexpr int kPreThreads = kAdjChunk / 8;
 
-// exclusive scan of the tile sums in one block: each thread a contiguous run
-// of tiles, then a scan of the threads' totals
-__global__ void __launch_bounds__(1024) k_scan_bsums(const int *seg, double *bsum)
+__global__ void __launch_bounds__(kPreThreads) k_adj_prefix(const int *seg, const int *cnt,
+                                                            const AdjLayout *L, const double *sE,
+                                                            const double *sg, double *pre)
 {
-    __shared__ double wtot[32][5];
-    const int nblocks = (seg[kMaterials] + kScanBlock - 1) / kScanBlock;
-    const int per = (nblocks + 1023) / 1024;
-    const int a = threadIdx.x * per, e = min(nblocks, a + per);
+    __shared__ double woff[kPreThreads / 32][10];
+    const int total = L->chunk_off[kMaterials];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int b = a; b < e; b++)
+    for (int gc = blockIdx.x; gc < total; gc += gridDim.x) {
+        int m = 0;
+        while (L->chunk_off[m + 1] <= gc) m++;
+        const int c = gc - L->chunk_off[m];
+        const long a = seg[m] + (long)c * kAdjChunk;
+        const long b = min((long)seg[m] + cnt[m], a + kAdjChunk);
+        const double eref = sE[a];
+        const long i0 = a + (long)threadIdx.x * 8, i1 = min(b, i0 + 8);
+        double v[10];
 #pragma unroll
-        for (int c = 0; c < 5; c++) tot[c] += bsum[(long)b * 5 + c];
-    double incl[5];
+        for (int k = 0; k < 10; k++) v[k] = 0.0;
+        for (long i = i0; i < i1; i++) {
+            const double de = sE[i] - eref;
 #pragma unroll
-    for (int c = 0; c < 5; c++) {
-        incl[c] = warp_incl(tot[c], lane);
-        if (lane == 31) wtot[warp][c] = incl[c];
-    }
-    __syncthreads();
-    if (threadIdx.x < 5) {   // exclusive scan of the 32 warp totals, in order
-        double run = 0.0;
-        for (int w = 0; w < 32; w++) {
-            const double v = wtot[w][threadIdx.x];
-            wtot[w][threadIdx.x] = run;
-            run += v;
+            for (int k = 0; k < 5; k++) {
+                const double g = sg[i * 5 + k];
+                v[k] += g;
+                v[5 + k] = fma(g, de, v[5 + k]);
+            }
         }
-    }
-    __syncthreads();
-    double run[5];
+        double incl[10];
 #pragma unroll
-    for (int c = 0; c < 5; c++) run[c] = wtot[warp][c] + (incl[c] - tot[c]);
-    for (int b = a; b < e; b++)
-#pragma unroll
-        for (int c = 0; c < 5; c++) {
-            const double v = bsum[(long)b * 5 + c];
-            bsum[(long)b * 5 + c] = run[c];
-            run[c] += v;
-        }
-}
-
-__global__ void __launch_bounds__(kScanThreads2) k_scan_local(const int *seg, const double *sg,
-                                                              const double *bsum, double *ep)
-{
-    __shared__ double sh[kScanBlock * 5];
-    __shared__ double woff[kScanThreads2 / 32][5];
-    const int total = seg[kMaterials];
-    const int nblocks = (total + kScanBlock - 1) / kScanBlock;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        const long tile0 = (long)b * kScanBlock;
-        scan_stage(sg, tile0, total, sh);
-        __syncthreads();
-        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int i = 0; i < kScanPer; i++) {
-            const double *x = sh + (threadIdx.x * kScanPer + i) * 5;
-#pragma unroll
-            for (int c = 0; c < 5; c++) v[c] += x[c];
-        }
-        double incl[5];
-#pragma unroll
-        for (int c = 0; c < 5; c++) {
-            incl[c] = warp_incl(v[c], lane);
-            if (lane == 31) woff[warp][c] = incl[c];
+        for (int k = 0; k < 10; k++) {
+            incl[k] = warp_incl(v[k], lane);
+            if (lane == 31) woff[warp][k] = incl[k];
         }
         __syncthreads();
-        if (threadIdx.x < 5) {   // exclusive offsets of the 8 warps, plus the tile's
-            double run = bsum[(long)b * 5 + threadIdx.x];
-            for (int w = 0; w < kScanThreads2 / 32; w++) {
+        if (threadIdx.x < 10) {
+            double run = 0.0;
+            for (int w = 0; w < kPreThreads / 32; w++) {
                 const double t = woff[w][threadIdx.x];
                 woff[w][threadIdx.x] = run;
                 run += t;
             }
         }
         __syncthreads();
-        double run[5];
+        double run[10];
 #pragma unroll
-        for (int c = 0; c < 5; c++) run[c] = woff[warp][c] + (incl[c] - v[c]);
-        // exclusive prefix of each of the thread's positions, in place
-        for (int i = 0; i < kScanPer; i++) {
-            double *x = sh + (threadIdx.x * kScanPer + i) * 5;
+        for (int k = 0; k < 10; k++) run[k] = woff[warp][k] + (incl[k] - v[k]);
+        double *out = pre + (a + gc) * 10;
+        for (long i = i0; i < i1; i++) {
+            double *o = out + (i - a) * 10;
+            const double de = sE[i] - eref;
 #pragma unroll
-            for (int c = 0; c < 5; c++) {
-                const double t = x[c];
-                x[c] = run[c];
-                run[c] += t;
+            for (int k = 0; k < 10; k++) o[k] = run[k];
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                const double g = sg[i * 5 + k];
+                run[k] += g;
+                run[5 + k] = fma(g, de, run[5 + k]);
             }
         }
-        // the prefix after the last position
-        const int last = total - 1 - (int)tile0;
-        if (last >= 0 && last / kScanPer == (int)threadIdx.x) {
-            // run[] now holds the inclusive prefix of this thread's last position;
-            // past the end of the data the staged zeros kept it unchanged
+        if (i1 == b && i0 < b) {
 #pragma unroll
-            for (int c = 0; c < 5; c++) ep[(long)total * 5 + c] = run[c];
+            for (int k = 0; k < 10; k++) out[(b - a) * 10 + k] = run[k];
         }
         __syncthreads();
-        const long base = tile0 * 5, end = (long)total * 5;
-        for (int i = threadIdx.x; i < kScanBlock * 5; i += kScanThreads2)
-            if (base + i < end) ep[base + i] = sh[i];
-        __syncthreads();
     }
-}
-
-// ---------------------------------------------------- transposed layout ---
-struct AdjLayout {
-    int nchunks[kMaterials];
-    int group[kMaterials];     // lanes per chunk (power of two >= num_nucs, <= 32)
-    int task_off[kMaterials + 1];
-    long slot_base[kMaterials];
-};
-
-__global__ void k_adj_layout(Tables t, const int *cnt, AdjLayout *L)
-{
-    if (threadIdx.x != 0) return;
-    int task = 0;
-    long slot = 0;
-    for (int m = 0; m < kMaterials; m++) {
-        const int nn = t.num_nucs[m];
-        int G = 1;
-        while (G < nn && G < 32) G <<= 1;
-        const int ngroups = (nn + G - 1) / G;
-        const int S = 32 / G;
-        const int nch = (cnt[m] + kAdjChunk - 1) / kAdjChunk;
-        L->nchunks[m] = nch;
-        L->group[m] = G;
-        L->task_off[m] = task;
-        L->slot_base[m] = slot;
-        task += nn ? ngroups * ((nch + S - 1) / S) : 0;
-        slot += (long)nn * nch * 2;
-    }
-    L->task_off[kMaterials] = task;
 }
 
 __device__ __forceinline__ void store10(double *dst, const double A[5], const double G[5])
@@ -333,12 +259,15 @@ __device__ __forceinline__ void store10(double *dst, const double A[5], const do
     }
 }
 
-// The transposed pass (see the file comment, step 4).
+// The transposed pass (see the file comment, step 4).  A lane takes one
+// nuclide of the chunk's material and walks the nuclide's intervals across
+// the chunk's sorted energies: the end of each interval's run of lookups is
+// found by a galloping search, and its sums come from the chunk-local
+// prefixes: G = dP_g, A = sum g (E_hi - E) = (E_hi - Eref) G - dP_gE.
 __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg, const int *cnt,
-                                                        const double *sE, const double *sg,
-                                                        const double *ep, const AdjLayout *L,
-                                                        unsigned int *queue, double *table,
-                                                        double *slots)
+                                                        const double *sE, const double *pre,
+                                                        const AdjLayout *L, unsigned int *queue,
+                                                        double *table, double *slots)
 {
     __shared__ AdjLayout lay;
     __shared__ int s_seg[kMaterials + 1], s_cnt[kMaterials];
@@ -348,6 +277,7 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const long n_int = t.n_gp - 1;
+    const long top = t.n_gp - 2;   // last interval
     for (;;) {
         unsigned int task = 0;
         if (lane == 0) task = atomicAdd(queue, 1u);
@@ -363,11 +293,14 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
         const int s = lane / G, jl = lane % G;
         const int j = grp * G + jl;
         const int c = cb * S + s;
-        if (j < nn && c < lay.nchunks[m]) {
+        if (j >= nn || c >= lay.nchunks[m]) continue;
         const long a = s_seg[m] + (long)c * kAdjChunk;
         const long b = min((long)s_seg[m] + s_cnt[m], a + kAdjChunk);
+        const double eref = sE[a];
+        const double *P = pre + (a + lay.chunk_off[m] + c) * 10;   // entry of position i: P[(i-a)*10]
         const int nuc = t.mats[m * t.max_nucs + j];
         const long long *ek = t.ekeys + (long)nuc * t.n_gp;
+        const xs_gridpoint *gp = t.grid + (long)nuc * t.n_gp;
         double *tab = table + ((long)(t.pair_base[m] + j) * n_int) * kTbl;
         double *slot = slots + (lay.slot_base[m] + ((long)j * lay.nchunks[m] + c) * 2) * kSlot;
 
@@ -382,51 +315,74 @@ __global__ void __launch_bounds__(256) k_adj_transposed(Tables t, const int *seg
             }
             k = lo - 1;
             if (k < 0) k = 0;
-            if (k > t.n_gp - 2) k = t.n_gp - 2;
+            if (k > top) k = top;
         }
         const long k_first = k;
-        long long next_key = (k + 1 <= t.n_gp - 2) ? ek[k + 1] : 0x7FFFFFFFFFFFFFFFLL;
-        double e_hi = t.grid[(long)nuc * t.n_gp + k + 1].energy;
-        double A[5] = {0, 0, 0, 0, 0}, Gs[5];
-        long i_start = a;   // first position of the current interval in this chunk
-        for (long i = a; i < b; i++) {
-            const double E = sE[i];
-            const long long q = order_key(E);
-            if (q >= next_key) {
-                // G over [i_start, i) from the prefix of gbar
+        long pos = a;
+        for (;;) {
+            // the run of interval k: [pos, end), end = first i with key(E_i) >= ek[k+1]
+            long end = b;
+            if (k < top) {
+                const long long nk = ek[k + 1];
+                long lo = pos, step = 1;   // key(E_lo) < nk
+                long hi = b;
+                for (;;) {
+                    const long probe = lo + step;
+                    if (probe >= b) break;
+                    if (order_key(sE[probe]) >= nk) {
+                        hi = probe;
+                        break;
+                    }
+                    lo = probe;
+                    step <<= 1;
+                }
+                while (hi - lo > 1) {
+                    const long mid = lo + ((hi - lo) >> 1);
+                    if (order_key(sE[mid]) >= nk) hi = mid; else lo = mid;
+                }
+                end = hi;
+            }
+            const double *p0 = P + (pos - a) * 10, *p1 = P + (end - a) * 10;
+            const double dh = gp[k + 1].energy - eref;
+            double A[5], Gs[5];
 #pragma unroll
-                for (int cc = 0; cc < 5; cc++) Gs[cc] = ep[i * 5 + cc] - ep[i_start * 5 + cc];
-                i_start = i;
-                // leave interval k: the first one goes to slot 0, later ones into the table
+            for (int cc = 0; cc < 5; cc++) {
+                Gs[cc] = p1[cc] - p0[cc];
+                A[cc] = fma(dh, Gs[cc], -(p1[5 + cc] - p0[5 + cc]));
+            }
+            if (end == b) {   // the chunk's last interval (possibly also its first)
                 if (k == k_first) {
                     slot[0] = __longlong_as_double(k);
                     store10(slot + 1, A, Gs);
+                    slot[kSlot] = __longlong_as_double(-1LL);
                 } else {
-                    store10(tab + k * kTbl, A, Gs);
+                    slot[kSlot] = __longlong_as_double(k);
+                    store10(slot + kSlot + 1, A, Gs);
                 }
-                do {
-                    k++;
-                    next_key = (k + 1 <= t.n_gp - 2) ? ek[k + 1] : 0x7FFFFFFFFFFFFFFFLL;
-                } while (q >= next_key);
-                e_hi = t.grid[(long)nuc * t.n_gp + k + 1].energy;
-#pragma unroll
-                for (int cc = 0; cc < 5; cc++) A[cc] = 0.0;
+                break;
             }
-            const double d = e_hi - E;
-            const double *g = sg + i * 5;
-#pragma unroll
-            for (int cc = 0; cc < 5; cc++) A[cc] = fma(g[cc], d, A[cc]);
-        }
-#pragma unroll
-        for (int cc = 0; cc < 5; cc++) Gs[cc] = ep[b * 5 + cc] - ep[i_start * 5 + cc];
-        if (k == k_first) {
-            slot[0] = __longlong_as_double(k);
-            store10(slot + 1, A, Gs);
-            slot[kSlot] = __longlong_as_double(-1LL);
-        } else {
-            slot[kSlot] = __longlong_as_double(k);
-            store10(slot + kSlot + 1, A, Gs);
-        }
+            if (k == k_first) {
+                slot[0] = __longlong_as_double(k);
+                store10(slot + 1, A, Gs);
+            } else {
+                store10(tab + k * kTbl, A, Gs);
+            }
+            // the interval of E_end: the largest j > k with ek[j] <= key(E_end),
+            // capped at the last interval (ek[k+1] <= key(E_end) here)
+            const long long q = order_key(sE[end]);
+            const long last = t.n_gp - 1;
+            long lo = k + 1, step = 1;   // ek[lo] <= q
+            while (lo + step <= last && ek[lo + step] <= q) {
+                lo += step;
+                step <<= 1;
+            }
+            long hi = min(lo + step, last + 1);   // ek[hi] > q, or hi == n_gp
+            while (hi - lo > 1) {
+                const long mid = lo + ((hi - lo) >> 1);
+                if (ek[mid] <= q) lo = mid; else hi = mid;
+            }
+            k = lo < top ? lo : top;
+            pos = end;
         }
     }
 }
@@ -573,8 +529,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     const size_t o_sE = off; off = align256(off + padded * 8);
     const size_t o_sid = off; off = align256(off + padded * 4);
     const size_t o_sg = off; off = align256(off + padded * 40);
-    const size_t o_ep = off; off = align256(off + (padded + 1) * 40);
-    const size_t o_bsum = off; off = align256(off + (padded / kScanBlock + 2) * 40);
+    const size_t o_pre = off; off = align256(off + (padded + count / kAdjChunk + kMaterials + 1) * 80);
     const size_t o_table = off; off = align256(off + (size_t)pairs * n_int * kTbl * 8);
     const size_t o_slots = off; off = align256(off + slot_count * kSlot * 8);
     const size_t need = off;
@@ -601,8 +556,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     double *sE = (double *)(B + o_sE);
     int *sid = (int *)(B + o_sid);
     double *sg = (double *)(B + o_sg);
-    double *ep = (double *)(B + o_ep);
-    double *bsum = (double *)(B + o_bsum);
+    double *pre = (double *)(B + o_pre);
     double *table = (double *)(B + o_table);
     double *slots = (double *)(B + o_slots);
 
@@ -639,15 +593,13 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
         XS_CUDA(cudaMemsetAsync(queue + 4, 0, 4, st));
         k_adj_layout<<<1, 32, 0, st>>>(t, cnt, L);
         XS_CUDA(cudaGetLastError());
-        k_scan_blocks<<<ctx->sm_count * 4, kScanThreads2, 0, st>>>(seg, sg, bsum);
-        k_scan_bsums<<<1, 1024, 0, st>>>(seg, bsum);
-        k_scan_local<<<ctx->sm_count * 4, kScanThreads2, 0, st>>>(seg, sg, bsum, ep);
+        k_adj_prefix<<<ctx->sm_count * 8, kPreThreads, 0, st>>>(seg, cnt, L, sE, sg, pre);
         XS_CUDA(cudaGetLastError());
-        k_adj_transposed<<<ctx->sm_count * 4, 256, 0, st>>>(t, seg, cnt, sE, sg, ep, L, queue + 4, table, slots);
+        k_adj_transposed<<<ctx->sm_count * 4, 256, 0, st>>>(t, seg, cnt, sE, pre, L, queue + 4, table, slots);
         XS_CUDA(cudaGetLastError());
         k_adj_fixup<<<ctx->sm_count * 8, 256, 0, st>>>(t, L, slots, table);
         XS_CUDA(cudaGetLastError());
-        n += 6;
+        n += 4;
         if (d_xs) {
             const long npts = (long)t.n_iso * t.n_gp;
             const long want = (npts + 255) / 256;
