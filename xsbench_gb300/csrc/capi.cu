@@ -336,7 +336,7 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
         t.mat_lo[m] = lo;
         t.mat_hi[m] = hi;
     }
-    {   // hot nuclides: most expected record accesses per lookup, within half of L2
+    {   // hot nuclides: most expected record accesses per lookup, within a quarter of L2
         double thr[kMaterials], prob[kMaterials];
         pick_mat_thresholds(thr);
         for (int m = 1; m < kMaterials; m++) prob[m] = thr[m] - thr[m - 1];
@@ -350,12 +350,12 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
         cudaDeviceProp prop;
         size_t l2 = 64u << 20;
         if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess && prop.l2CacheSize > 0) l2 = (size_t)prop.l2CacheSize;
-        double frac = 0.5;
+        double frac = 0.25;
         if (const char *env = getenv("XSGB_HOT_FRACTION")) {
             const double v = atof(env);
             if (v >= 0.0 && v <= 1.0) frac = v;
         }
-        const size_t per = (size_t)(in->n_gridpoints - 1) * 96, budget = (size_t)(l2 * frac);
+        const size_t per = (size_t)(in->n_gridpoints - 1) * kRecordDoubles * 8, budget = (size_t)(l2 * frac);
         t.cold_normal = 0;
         if (const char *env = getenv("XSGB_L2_COLD")) t.cold_normal = strcmp(env, "normal") == 0;
         size_t used = 0;

@@ -275,13 +275,14 @@ __device__ __forceinline__ double2 ld_v2(const double2 *p, unsigned long long po
     return v;
 }
 
-// FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record, read
+// FAST: xs = hi - (E_hi - E) * slope from the 96-byte interval record (in its
+// 128-byte slot), read
 // with three 32-byte loads (a record is three aligned sectors).
 template <bool DE = false>
 __device__ __forceinline__ void accumulate_fast(const Tables &t, int nuc, long k, double E,
                                                 double conc, double macro[5], double *S = nullptr)
 {
-    const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * 6);
+    const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * kRecordPairs);
     const unsigned long long pol = record_policy(t, nuc);
     double e_hi, h0, h1, h2, h3, h4, s0, s1, s2, s3, s4, e_lo;
     ld_v4(r, e_hi, h0, h1, h2, pol);
@@ -340,7 +341,7 @@ template <int ARITH>
 __device__ __forceinline__ const void *interval_bytes(const Tables &t, int nuc, long k)
 {
     if (ARITH == XS_ARITH_EXACT) return t.grid + (long)nuc * t.n_gp + k;
-    return t.records + ((long)nuc * (t.n_gp - 1) + k) * 6;
+    return t.records + ((long)nuc * (t.n_gp - 1) + k) * kRecordPairs;
 }
 
 #ifndef XSGB_PIPE_P

@@ -3,7 +3,8 @@
 // index without bounds checks.
 //
 //   records     per nuclide interval k: E_hi, the five xs at k+1, the five
-//               slopes (xs_{k+1}-xs_k)/(E_{k+1}-E_k) and E_lo (96 bytes)
+//               slopes (xs_{k+1}-xs_k)/(E_{k+1}-E_k) and E_lo (96 bytes in a
+//               128-byte slot)
 //   ekeys       order keys of every gridpoint energy (HASH / NUCLIDE searches)
 //   coarse      every 16th key of each nuclide (NUCLIDE search, first level)
 //   union_keys  order keys of the unionized energies
@@ -28,7 +29,7 @@ __global__ void k_records(const xs_gridpoint *grid, long n_iso, long n_gp, doubl
         const xs_gridpoint lo = grid[nuc * n_gp + k];
         const xs_gridpoint hi = grid[nuc * n_gp + k + 1];
         const double dE = hi.energy - lo.energy;
-        double2 *r = rec + i * 6;
+        double2 *r = rec + i * kRecordPairs;
         r[0] = make_double2(hi.energy, hi.total_xs);
         r[1] = make_double2(hi.elastic_xs, hi.absorbtion_xs);
         r[2] = make_double2(hi.fission_xs, hi.nu_fission_xs);
@@ -36,6 +37,8 @@ __global__ void k_records(const xs_gridpoint *grid, long n_iso, long n_gp, doubl
         r[4] = make_double2((hi.absorbtion_xs - lo.absorbtion_xs) / dE,
                             (hi.fission_xs - lo.fission_xs) / dE);
         r[5] = make_double2((hi.nu_fission_xs - lo.nu_fission_xs) / dE, lo.energy);
+        r[6] = make_double2(0.0, 0.0);   // slot padding
+        r[7] = make_double2(0.0, 0.0);
     }
 }
 
@@ -110,7 +113,7 @@ __global__ void k_union_table(Tables t, int m, int n_m, double2 *out)
         const int nuc = t.mats[m * t.max_nucs + j];
         long k = t.index_grid[e * t.n_iso + nuc];
         if (k == top) k -= 1;
-        const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * 6);
+        const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * kRecordPairs);
         const double d = t.union_e[e] - r[0];
         double2 *o = out + i * 5;
 #pragma unroll
@@ -172,7 +175,7 @@ xs_status build_derived_tables(xs_ctx *ctx)
 
     // interval records for the fast arithmetic
     void *p = nullptr;
-    xs_status s = ctx_alloc(ctx, &p, (size_t)t.n_iso * (t.n_gp - 1) * 96);
+    xs_status s = ctx_alloc(ctx, &p, (size_t)t.n_iso * (t.n_gp - 1) * kRecordDoubles * 8);
     if (s != XS_OK) return s;
     t.records = (const double2 *)p;
     k_records<<<grid_for(t.n_iso * (t.n_gp - 1), sm), 256, 0, st>>>(t.grid, t.n_iso, t.n_gp, (double2 *)p);
