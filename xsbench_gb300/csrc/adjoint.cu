@@ -584,6 +584,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     l.err = ctx->s.error;
     l.fuel_lanes = 1;
     l.table = 1;   // the forward reads the union table when there is one
+    l.sorted = 1;
     s = launch_adjoint_energy(ctx, st, l, sg, d_energy);
     if (s != XS_OK) return s;
 

@@ -391,6 +391,12 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
     // union table (set by build_union_table); xs_autotune measures 1, 2 and 4;
     // XSGB_FUEL_LANES and XSGB_BATCHED_FUEL_LANES = 1, 2 or 4 override
     for (int m = 0; m < kMaterials; m++) ctx->num_nucs_host[m] = sd->num_nucs[m];
+    // energy buckets of the batched sort: at least one per 8 gridpoints of a
+    // nuclide, so that a warp's 32 sorted lookups span few intervals (the
+    // warp-cooperative nuclide search holds 32 keys)
+    ctx->batched_buckets = 4096;
+    while (ctx->batched_buckets < 65536 && (long)ctx->batched_buckets * 8 < in->n_gridpoints)
+        ctx->batched_buckets <<= 1;
     // (measured: 4 lanes win up to ~11,000 gridpoints per nuclide and lose on
     // the 238,847-point XL grid)
     ctx->fuel_lanes = (sd->num_nucs[0] >= 64 && in->n_gridpoints <= 65536) ? 4 : 1;

@@ -164,6 +164,61 @@ __device__ __forceinline__ long interval_nuclide(const Tables &t, int nuc, long 
     return kk;
 }
 
+// Warp-cooperative form of the same count, for a batch whose warp holds
+// lookups of one material within a narrow energy range (the batched kernel):
+// #{ek[0..n) <= q} for a warp-uniform q by a 32-ary search (each round the 32
+// lanes probe 32 evenly spaced keys and a ballot keeps one of the 32 pieces),
+// 4 dependent loads for 238,847 keys instead of 18.  Every lane must call it.
+__device__ __forceinline__ long warp_count_le(const long long *ek, long n, long long q, int lane)
+{
+    long lo = 0, hi = n;   // the count lies in [lo, hi]
+    while (hi - lo > 32) {
+        const long step = (hi - lo + 31) >> 5;
+        const long p = lo + (long)(lane + 1) * step - 1;
+        const bool le = p < hi && ldg(&ek[p]) <= q;
+        const long c = __popc(__ballot_sync(0xffffffffu, le));
+        const long nhi = lo + (c + 1) * step - 1;
+        hi = nhi < hi ? nhi : hi;
+        lo = lo + c * step;
+    }
+    const long p = lo + lane;
+    const bool le = p < hi && ldg(&ek[p]) <= q;
+    return lo + __popc(__ballot_sync(0xffffffffu, le));
+}
+
+// NUCLIDE interval of each lane's key q (live lanes' keys in [qmin, qmax],
+// warp-uniform bounds): the count for qmin cooperatively, then the 32 keys
+// from there held one per lane; when they cover qmax every lane finds its own
+// count by binary lifting over the window with shuffles, otherwise by its own
+// search.  The same interval as interval_nuclide.
+__device__ __forceinline__ long interval_nuclide_warp(const Tables &t, int nuc, long long q,
+                                                      long long qmin, long long qmax, int lane)
+{
+    const long n = t.n_gp;
+    const long long *ek = t.ekeys + (long)nuc * n;
+    const long c0 = warp_count_le(ek, n, qmin, lane);
+    const long wi = c0 + lane;
+    const long long wkey = wi < n ? ldg(&ek[wi]) : 0x7FFFFFFFFFFFFFFFLL;
+    const long long cap = c0 + 32 < n ? ldg(&ek[c0 + 32]) : 0x7FFFFFFFFFFFFFFFLL;
+    long cnt;
+    if (cap > qmax) {   // every live lane's count is in [c0, c0 + 32]
+        int pos = 0;
+#pragma unroll
+        for (int step = 32; step >= 1; step >>= 1) {
+            const int probe = pos + step;
+            const long long key = __shfl_sync(0xffffffffu, wkey, (probe - 1) & 31);
+            if (probe <= 32 && key <= q) pos = probe;
+        }
+        cnt = c0 + pos;
+    } else {
+        return interval_nuclide(t, nuc, q);
+    }
+    long kk = cnt - 1;
+    if (kk < 0) kk = 0;
+    if (kk > n - 2) kk = n - 2;
+    return kk;
+}
+
 // HASH (Simulation.c:273-302), including its edge rules: E <= e_low gives
 // gridpoint 0, E >= e_high gives the last interval.
 template <bool CHECKED>
@@ -444,6 +499,33 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
                 else
                     accumulate_fast<DE>(t, nuc, k, E, conc, macro, S);
             }
+        }
+    }
+}
+
+// NUCLIDE lookup of one warp of a batch (every lane calls; `live` lanes
+// accumulate; qmin / qmax bound the live lanes' keys, warp-uniform; no NaN).
+template <int ARITH, bool CHECKED>
+__device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E, int mat, bool live,
+                                                      long long qmin, long long qmax,
+                                                      double macro[5], int *err)
+{
+#pragma unroll
+    for (int c = 0; c < 5; c++) macro[c] = 0.0;
+    const int n = ldg(&t.num_nucs[mat]);
+    const int *mrow = t.mats + mat * t.max_nucs;
+    const double *crow = t.concs + mat * t.max_nucs;
+    const long long q = order_key(E);
+    const int lane = threadIdx.x & 31;
+    for (int j = 0; j < n; j++) {
+        const int nuc = ldg(&mrow[j]);
+        const double conc = ldg(&crow[j]);
+        const long k = interval_nuclide_warp(t, nuc, q, qmin, qmax, lane);
+        if (live) {
+            if (ARITH == XS_ARITH_EXACT)
+                accumulate_exact(t, nuc, k, E, conc, macro);
+            else
+                accumulate_fast<false>(t, nuc, k, E, conc, macro, nullptr);
         }
     }
 }

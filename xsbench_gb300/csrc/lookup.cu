@@ -267,6 +267,7 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
         l.err = ctx->s.error;
         l.fuel_lanes = ctx->fuel_lanes;  // the plain kernel's arithmetic, lookup for lookup
         l.table = 0;
+        l.sorted = 0;
         XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
                                           ctx->sm_count * ctx->batched_blocks_per_sm, l));
         if (launches) *launches += 2;
@@ -337,6 +338,7 @@ xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int check
     l.err = b.error;
     l.fuel_lanes = ctx->batched_fuel_lanes;
     l.table = 1;
+    l.sorted = 1;
     XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
                                       ctx->sm_count * ctx->batched_blocks_per_sm, l));
     if (launches) *launches += 4;
@@ -427,6 +429,7 @@ xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first
     l.err = b.error;
     l.fuel_lanes = ctx->batched_fuel_lanes;
     l.table = 1;
+    l.sorted = 1;
     XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, 0,
                                       ctx->sm_count * ctx->batched_blocks_per_sm, l));
     return XS_OK;

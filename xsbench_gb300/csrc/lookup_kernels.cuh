@@ -55,6 +55,7 @@ struct ListArgs {
     int *err;
     int fuel_lanes;              // lanes per fuel lookup (PlainArgs::fuel_lanes)
     int table;                   // 1: read the union table when there is one (FAST)
+    int sorted;                  // 1: entries sorted by energy bucket (warp searches pay)
 };
 
 // Adds the per-lane verification counts of a block into *verif (one atomic).
@@ -126,6 +127,43 @@ __device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool
         for (int k = 0; k < 5; k++) macro[k] += __shfl_xor_sync(0xffffffffu, macro[k], s);
     }
     if (!live || q != 0) return 0;
+    const int arg = argmax5(macro);
+    if (out_macro) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
+    }
+    if (out_idx) out_idx[o] = (unsigned char)arg;
+    return (unsigned)(arg + 1);
+}
+
+// A warp's 32 entries of one material on the NUCLIDE grid, sorted by energy
+// bucket: the warp-cooperative interval search (macro_xs_nuclide_warp) when no
+// live energy is NaN, else each lane's own lookup.  Every lane calls this.
+template <int ARITH, bool CHECKED>
+__device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &t, bool live,
+                                                                  double E, int m, long o,
+                                                                  double *out_macro,
+                                                                  unsigned char *out_idx,
+                                                                  int *err)
+{
+    const unsigned full = 0xffffffffu;
+    const bool keyed = !(E != E);
+    if (!__any_sync(full, live)) return 0;
+    if (!__all_sync(full, !live || keyed)) {
+        if (!live) return 0;
+        return lookup_and_store<XS_NUCLIDE, ARITH, CHECKED, false>(t, E, m, o, out_macro, out_idx, err);
+    }
+    const long long q = order_key(E);
+    long long qmin = live ? q : 0x7FFFFFFFFFFFFFFFLL, qmax = live ? q : (-0x7FFFFFFFFFFFFFFFLL - 1);
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const long long a = __shfl_xor_sync(full, qmin, s), b = __shfl_xor_sync(full, qmax, s);
+        qmin = a < qmin ? a : qmin;
+        qmax = b > qmax ? b : qmax;
+    }
+    double macro[5];
+    macro_xs_nuclide_warp<ARITH, CHECKED>(t, E, m, live, qmin, qmax, macro, err);
+    if (!live) return 0;
     const int arg = argmax5(macro);
     if (out_macro) {
 #pragma unroll
@@ -313,6 +351,16 @@ __device__ __forceinline__ void list_lookup_body(const Tables &t, const ListArgs
         const int pv = cv * 32 + lane;
         int m = 0;
         while (seg[m + 1] <= cv * 32) m++;
+        if constexpr (GRID == XS_NUCLIDE) {
+            if (a.sorted) {
+                const bool live = pv < seg[m] + cnt[m];
+                const long p = live ? (long)bas[m] + (pv - seg[m]) : 0;
+                mine += nuclide_warp_lookup_and_store<ARITH, CHECKED>(
+                    t, live, live ? a.E[p] : 0.0, m, live ? (long)a.id[p] : 0, a.out_macro,
+                    a.out_idx, a.err);
+                continue;
+            }
+        }
         if (pv < seg[m] + cnt[m]) {
             const long p = (long)bas[m] + (pv - seg[m]);
             mine += lookup_and_store<GRID, ARITH, CHECKED, TABLE>(t, a.E[p], m, a.id[p], a.out_macro,
