@@ -78,6 +78,12 @@ def algorithmic_bytes_per_lookup(inputs, num_nucs) -> float:
     return nbar * (8 * math.ceil(math.log2(n_gp)) + 96)
 
 
+def nbar_of(inputs, problem) -> float:
+    """Expected nuclides per lookup (material probabilities x list lengths)."""
+    nn = list(problem.arrays()["num_nucs"])
+    return sum(p * n for p, n in zip(material_probabilities(), nn))
+
+
 def measured_peak_gbs():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -419,6 +425,15 @@ def main():
                          "algorithmic_bytes_per_lookup": bpl,
                          "traffic": (traffic_pl * N if traffic_pl else None),
                          "traffic_source": traffic_src},
+            # the other bound of this FP64 path: 11 FP64 instructions per nuclide
+            # (FAST records: one subtraction, five interpolations, five
+            # accumulations) against GB300's FP64 rate (1.25 TFLOP/s nominal =
+            # 625 G fused multiply-adds per second)
+            "fp64": ({"ops_per_lookup": round(11 * nbar_of(inputs, problem), 1),
+                      "achieved_gops": value * 11 * nbar_of(inputs, problem) / 1e9,
+                      "peak_gops": 625.0, "peak_source": "nominal GB300 FP64 FMA rate",
+                      "frac": value * 11 * nbar_of(inputs, problem) / 625e9}
+                     if args.arith == "fast" and args.kernel == "plain" else None),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 12,
                     "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",
                     "verification_matches": bool(e2e_ok)},
