@@ -267,34 +267,21 @@ __device__ __forceinline__ unsigned long long policy_first()
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
-__device__ __forceinline__ unsigned long long policy_normal()
-{
-    unsigned long long p;
-    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
 __device__ __forceinline__ bool is_hot(const Tables &t, int nuc)
 {
     return nuc < 512 && ((t.hot[nuc >> 5] >> (nuc & 31)) & 1u);
 }
 __device__ __forceinline__ unsigned long long record_policy(const Tables &t, int nuc)
 {
-    return is_hot(t, nuc) ? policy_last() : (t.cold_normal ? policy_normal() : policy_first());
+    return is_hot(t, nuc) ? policy_last() : policy_first();
 }
-#ifndef XSGB_PREFETCH_POL
-#define XSGB_PREFETCH_POL 2
-#endif
-// Policy of the L2 prefetch of a record that the lane reads a nuclide later:
+// Policy of the L2 prefetch of a record that the lane reads one nuclide later:
 // evict_last, so the line survives until that load, which reads it with
-// record_policy (evict_first for the cold records) and so releases it.
-// 0: record_policy, 1: evict_normal, 2: evict_last (default; 2.5 % fewer
-// DRAM bytes than 0).
-__device__ __forceinline__ unsigned long long prefetch_policy(const Tables &t, int nuc)
+// record_policy (evict_first for the cold records) and so releases it
+// (2.5 % less DRAM traffic than prefetching under record_policy).
+__device__ __forceinline__ unsigned long long prefetch_policy(const Tables &, int)
 {
-    if (is_hot(t, nuc)) return policy_last();
-    if (XSGB_PREFETCH_POL == 1) return policy_normal();
-    if (XSGB_PREFETCH_POL == 2) return policy_last();
-    return t.cold_normal ? policy_normal() : policy_first();
+    return policy_last();
 }
 
 // ------------------------------------------------------------- prefetch ---

@@ -51,7 +51,6 @@ struct Tables {
     int mat_lo[kMaterials];          // smallest / largest nuclide id of each material
     int mat_hi[kMaterials];          //   (span of the index-row prefetch)
     unsigned hot[16];                // nuclides (< 512) whose records stay in L2 (evict_last)
-    int cold_normal;                 // 1: the other records evict_normal instead of evict_first
     int pair_base[kMaterials + 1];   // running sum of num_nucs: (material, position) pairs
     const int *inv_off;              // [n_iso + 1] pairs holding each nuclide (CSR)
     const int *inv_pair;             // [pairs] m * max_nucs + j, by nuclide, m ascending
