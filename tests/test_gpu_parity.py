@@ -225,6 +225,37 @@ def test_history_small_particles():
             assert r.verification == g["particles_2000_verification"], arith
 
 
+@pytest.mark.parametrize("size", ["small", "large"])
+def test_history_full_published_hash(size):
+    """History-based mode at the reference's default size (500,000 particles x
+    34 lookups): the published hashes 941535 / 954318 (io.c:94-95)."""
+    g = golden_json("history_" + size)
+    inp = X.make_inputs(size=size, grid="unionized", method="history")
+    assert inp.particles == g["particles"] and inp.lookups == g["lookups"]
+    with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
+        for arith in ("fast", "exact"):
+            r = ctx.run_history(arith=arith)
+            assert r.verification == g["verification"], arith
+            assert r.verification % 999983 == g["hash"]
+
+
+@pytest.mark.parametrize("args,expect", [
+    (["-m", "event", "-s", "small", "-k", "0"], 945990),
+    (["-m", "event", "-s", "small", "-k", "1"], 945990),
+    (["-m", "event", "-s", "small", "-k", "2"], 945990),
+    (["-m", "event", "-s", "small", "-G", "hash", "-k", "3"], 945990),
+    (["-m", "history", "-s", "small"], 941535),
+])
+def test_c_driver_reports_the_published_hash(args, expect):
+    """The C host program (the reference's main over the C ABI) exits 0 and
+    prints the reference's verification value."""
+    import subprocess
+    from xsbench_gb300 import build as B
+    out = subprocess.run([B.EXE_PATH, *args], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert str(expect) in out.stdout
+
+
 def test_drop_in_seam():
     g = golden_json("full_tiny_unionized")
     inp = product_inputs("tiny_unionized")
