@@ -169,9 +169,10 @@ __device__ __forceinline__ long interval_nuclide(const Tables &t, int nuc, long 
 // #{ek[0..n) <= q} for a warp-uniform q by a 32-ary search (each round the 32
 // lanes probe 32 evenly spaced keys and a ballot keeps one of the 32 pieces),
 // 4 dependent loads for 238,847 keys instead of 18.  Every lane must call it.
-__device__ __forceinline__ long warp_count_le(const long long *ek, long n, long long q, int lane)
+__device__ __forceinline__ long warp_count_le(const long long *ek, long lo, long hi, long long q,
+                                              int lane)
 {
-    long lo = 0, hi = n;   // the count lies in [lo, hi]
+    // the count lies in [lo, hi]
     while (hi - lo > 32) {
         const long step = (hi - lo + 31) >> 5;
         const long p = lo + (long)(lane + 1) * step - 1;
@@ -190,13 +191,31 @@ __device__ __forceinline__ long warp_count_le(const long long *ek, long n, long 
 // warp-uniform bounds): the count for qmin cooperatively, then the 32 keys
 // from there held one per lane; when they cover qmax every lane finds its own
 // count by binary lifting over the window with shuffles, otherwise by its own
-// search.  The same interval as interval_nuclide.
+// binary search past that count (no coarse keys: every grid type has ekeys).
+// The same interval as interval_nuclide.
+//
+// bin_min >= 0 (hash grid): qmin's energy lies in hash bin bin_min, so its
+// count lies between the bin's index entries (the warp-cooperative hash-bin
+// search: one ballot over the bin's keys); -1: search all n keys.  `eq`
+// returns whether the key below the count equals q (the hash edge rule).
 __device__ __forceinline__ long interval_nuclide_warp(const Tables &t, int nuc, long long q,
-                                                      long long qmin, long long qmax, int lane)
+                                                      long long qmin, long long qmax, int lane,
+                                                      long bin_min, bool &eq)
 {
     const long n = t.n_gp;
     const long long *ek = t.ekeys + (long)nuc * n;
-    const long c0 = warp_count_le(ek, n, qmin, lane);
+    long lo = 0, hi = n;
+    if (bin_min >= 0) {
+        // u_low = clamp(#{E_j <= bin edge} - 1, 0, n - 2) <= the count; the count
+        // is at most #{E_j <= next edge} = next entry + 1 unless that entry is clamped
+        lo = ldg(&t.index_grid[bin_min * t.n_iso + nuc]);
+        if (bin_min < t.hash_bins - 1) {
+            const long nx = ldg(&t.index_grid[(bin_min + 1) * t.n_iso + nuc]);
+            if (nx < n - 2) hi = nx + 1;
+        }
+    }
+    const long c0 = warp_count_le(ek, lo, hi, qmin, lane);
+    const long long below = c0 > 0 ? ldg(&ek[c0 - 1]) : (-0x7FFFFFFFFFFFFFFFLL - 1);
     const long wi = c0 + lane;
     const long long wkey = wi < n ? ldg(&ek[wi]) : 0x7FFFFFFFFFFFFFFFLL;
     const long long cap = c0 + 32 < n ? ldg(&ek[c0 + 32]) : 0x7FFFFFFFFFFFFFFFLL;
@@ -209,9 +228,17 @@ __device__ __forceinline__ long interval_nuclide_warp(const Tables &t, int nuc, 
             const long long key = __shfl_sync(0xffffffffu, wkey, (probe - 1) & 31);
             if (probe <= 32 && key <= q) pos = probe;
         }
+        const long long kb = __shfl_sync(0xffffffffu, wkey, (pos - 1) & 31);
+        eq = (pos > 0 ? kb : below) == q;
         cnt = c0 + pos;
-    } else {
-        return interval_nuclide(t, nuc, q);
+    } else {   // the warp's energies span more than 32 keys: each lane searches past c0
+        long a = c0, b = n;
+        while (a < b) {
+            const long mid = (a + b) >> 1;
+            if (ldg(&ek[mid]) <= q) a = mid + 1; else b = mid;
+        }
+        cnt = a;
+        eq = (cnt > c0 ? ldg(&ek[cnt - 1]) : below) == q;
     }
     long kk = cnt - 1;
     if (kk < 0) kk = 0;
@@ -490,9 +517,16 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
     }
 }
 
-// NUCLIDE lookup of one warp of a batch (every lane calls; `live` lanes
-// accumulate; qmin / qmax bound the live lanes' keys, warp-uniform; no NaN).
-template <int ARITH, bool CHECKED>
+// NUCLIDE (or HASH) lookup of one warp of a batch (every lane calls; `live`
+// lanes accumulate; qmin / qmax bound the live lanes' keys, warp-uniform; no
+// NaN).  The cooperative search gives the bracketing interval.  The hash
+// lookup (Simulation.c:273-301) gives the same interval whenever E lies in
+// its bin, [bin*du, (bin+1)*du), except by its edge rule E <= E[u_low] ->
+// gridpoint 0, which then holds only when E equals a gridpoint: that case
+// loads u_low and applies the rule.  A lookup whose E / du rounded it into a
+// neighbouring bin (E within an ulp of a bin edge) takes the hash search
+// itself (interval_hash) for every nuclide.
+template <int ARITH, bool CHECKED, bool HASHQ = false>
 __device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E, int mat, bool live,
                                                       long long qmin, long long qmax,
                                                       double macro[5], int *err)
@@ -504,10 +538,35 @@ __device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E,
     const double *crow = t.concs + mat * t.max_nucs;
     const long long q = order_key(E);
     const int lane = threadIdx.x & 31;
+    long bin = 0, bin_min = -1;
+    bool outside = false;   // E not in [bin*du, (bin+1)*du)
+    if (HASHQ) {
+        bin = (long)(E / t.hash_du);   // Simulation.c:350-351
+        if (bin < 0) bin = 0;
+        if (bin > t.hash_bins - 1) bin = t.hash_bins - 1;
+        outside = (double)bin * t.hash_du > E ||
+                  (bin < t.hash_bins - 1 && (double)(bin + 1) * t.hash_du <= E);
+        // the bin of the warp's lowest live energy, when that energy lies in it
+        const bool is_min = live && q == qmin;
+        const unsigned owners = __ballot_sync(0xffffffffu, is_min);
+        const int src = __ffs(owners) - 1;
+        const long b0 = __shfl_sync(0xffffffffu, bin, src < 0 ? 0 : src);
+        const bool out0 = __shfl_sync(0xffffffffu, outside, src < 0 ? 0 : src);
+        bin_min = (src >= 0 && !out0) ? b0 : -1;
+    }
     for (int j = 0; j < n; j++) {
         const int nuc = ldg(&mrow[j]);
         const double conc = ldg(&crow[j]);
-        const long k = interval_nuclide_warp(t, nuc, q, qmin, qmax, lane);
+        bool eq = false;
+        long k = interval_nuclide_warp(t, nuc, q, qmin, qmax, lane, bin_min, eq);
+        if (HASHQ && live) {
+            if (outside) {
+                k = interval_hash<false>(t, bin, nuc, q, err);
+            } else if (eq && k > 0) {
+                const long ul = ldg(&t.index_grid[bin * t.n_iso + nuc]);
+                if (q <= ldg(&t.ekeys[(long)nuc * t.n_gp + ul])) k = 0;
+            }
+        }
         if (live) {
             if (ARITH == XS_ARITH_EXACT)
                 accumulate_exact(t, nuc, k, E, conc, macro);

@@ -136,10 +136,11 @@ __device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool
     return (unsigned)(arg + 1);
 }
 
-// A warp's 32 entries of one material on the NUCLIDE grid, sorted by energy
-// bucket: the warp-cooperative interval search (macro_xs_nuclide_warp) when no
-// live energy is NaN, else each lane's own lookup.  Every lane calls this.
-template <int ARITH, bool CHECKED>
+// A warp's 32 entries of one material on the NUCLIDE or HASH grid, sorted by
+// energy bucket: the warp-cooperative interval search (macro_xs_nuclide_warp)
+// when no live energy is NaN, else each lane's own lookup.  Every lane calls
+// this.
+template <int GRID, int ARITH, bool CHECKED>
 __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &t, bool live,
                                                                   double E, int m, long o,
                                                                   double *out_macro,
@@ -151,7 +152,7 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
     if (!__any_sync(full, live)) return 0;
     if (!__all_sync(full, !live || keyed)) {
         if (!live) return 0;
-        return lookup_and_store<XS_NUCLIDE, ARITH, CHECKED, false>(t, E, m, o, out_macro, out_idx, err);
+        return lookup_and_store<GRID, ARITH, CHECKED, false>(t, E, m, o, out_macro, out_idx, err);
     }
     const long long q = order_key(E);
     long long qmin = live ? q : 0x7FFFFFFFFFFFFFFFLL, qmax = live ? q : (-0x7FFFFFFFFFFFFFFFLL - 1);
@@ -162,7 +163,7 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
         qmax = b > qmax ? b : qmax;
     }
     double macro[5];
-    macro_xs_nuclide_warp<ARITH, CHECKED>(t, E, m, live, qmin, qmax, macro, err);
+    macro_xs_nuclide_warp<ARITH, CHECKED, GRID == XS_HASH>(t, E, m, live, qmin, qmax, macro, err);
     if (!live) return 0;
     const int arg = argmax5(macro);
     if (out_macro) {
@@ -187,7 +188,7 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
 // different row of a table of ~155 GB, and the page-translation misses of that
 // pattern cost more than the bytes it saves (the batched kernel, whose warps
 // read neighbouring rows, uses it).
-template <int GRID, int ARITH, bool CHECKED, bool SAMPLES, bool TABLE = false>
+template <int GRID, int ARITH, bool CHECKED, bool SAMPLES>
 __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables t, PlainArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
             const int p = (int)c * (32 / L) + lane / L;
             const bool live = p < (overflow ? (cnt[0] & ~31) : cnt[0]);
             const int l = live ? perm[p] : 0;
-            mine += split_lookup_and_store<GRID, CHECKED, TABLE>(t, live, sE[l], base + l, q, L,
+            mine += split_lookup_and_store<GRID, CHECKED, false>(t, live, sE[l], base + l, q, L,
                                                                  a.out_macro, a.out_idx, a.err);
             continue;
         }
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
         const int limit = seg[m] + (overflow ? (cnt[m] & ~31) : cnt[m]);
         if (p < limit) {
             const int l = perm[p];
-            mine += lookup_and_store<GRID, ARITH, CHECKED, TABLE>(t, sE[l], m, base + l, a.out_macro,
+            mine += lookup_and_store<GRID, ARITH, CHECKED, false>(t, sE[l], m, base + l, a.out_macro,
                                                                   a.out_idx, a.err);
         }
     }
@@ -351,11 +352,11 @@ __device__ __forceinline__ void list_lookup_body(const Tables &t, const ListArgs
         const int pv = cv * 32 + lane;
         int m = 0;
         while (seg[m + 1] <= cv * 32) m++;
-        if constexpr (GRID == XS_NUCLIDE) {
-            if (a.sorted) {
+        if constexpr (GRID == XS_NUCLIDE || GRID == XS_HASH) {
+            if (a.sorted && !CHECKED) {
                 const bool live = pv < seg[m] + cnt[m];
                 const long p = live ? (long)bas[m] + (pv - seg[m]) : 0;
-                mine += nuclide_warp_lookup_and_store<ARITH, CHECKED>(
+                mine += nuclide_warp_lookup_and_store<GRID, ARITH, CHECKED>(
                     t, live, live ? a.E[p] : 0.0, m, live ? (long)a.id[p] : 0, a.out_macro,
                     a.out_idx, a.err);
                 continue;
