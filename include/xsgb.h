@@ -222,7 +222,13 @@ xs_status xs_lookup_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *
                             unsigned char *max_idx_out, xs_run_result *result);
 
 /* History-based lookups (openmp-threading/Simulation.c:116-238) for particles
- * [first, first+count) of opts (count <= 0: inputs.particles). */
+ * [first, first+count) of opts (count <= 0: inputs.particles).  PLAIN: one
+ * thread per particle walks its lookups, as the reference does.  BATCHED: the
+ * particles advance in lockstep, step by step: the i-th lookups of all
+ * particles run as one event batch through the plain lookup kernel, then each
+ * particle's next sample is drawn (the same seeds, skips and samples as the
+ * reference's loop), so material sorting and load balance apply to history
+ * mode too. */
 xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *result);
 
 /* Adjoint of the lookup (no reference counterpart: the reference has no

@@ -220,9 +220,14 @@ def test_history_small_particles():
     inp = X.make_inputs(size="small", grid="unionized", method="history", lookups=34,
                         particles=2000)
     with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
-        for arith in ("exact", "fast"):
-            r = ctx.run_history(arith=arith)
-            assert r.verification == g["particles_2000_verification"], arith
+        for kernel in ("plain", "batched"):
+            for arith in ("exact", "fast"):
+                r = ctx.run_history(kernel=kernel, arith=arith)
+                assert r.verification == g["particles_2000_verification"], (kernel, arith)
+        # a range of particles, stepped, adds up with the rest
+        a = ctx.run_history(kernel="batched", first=0, count=777).verification
+        b = ctx.run_history(kernel="batched", first=777, count=2000 - 777).verification
+        assert a + b == g["particles_2000_verification"]
 
 
 @pytest.mark.parametrize("size", ["small", "large"])
@@ -233,10 +238,11 @@ def test_history_full_published_hash(size):
     inp = X.make_inputs(size=size, grid="unionized", method="history")
     assert inp.particles == g["particles"] and inp.lookups == g["lookups"]
     with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
-        for arith in ("fast", "exact"):
-            r = ctx.run_history(arith=arith)
-            assert r.verification == g["verification"], arith
-            assert r.verification % 999983 == g["hash"]
+        for kernel in ("plain", "batched"):
+            for arith in ("fast", "exact"):
+                r = ctx.run_history(kernel=kernel, arith=arith)
+                assert r.verification == g["verification"], (kernel, arith)
+                assert r.verification % 999983 == g["hash"]
 
 
 @pytest.mark.parametrize("args,expect", [
@@ -245,6 +251,7 @@ def test_history_full_published_hash(size):
     (["-m", "event", "-s", "small", "-k", "2"], 945990),
     (["-m", "event", "-s", "small", "-G", "hash", "-k", "3"], 945990),
     (["-m", "history", "-s", "small"], 941535),
+    (["-m", "history", "-s", "small", "-k", "1"], 941535),
 ])
 def test_c_driver_reports_the_published_hash(args, expect):
     """The C host program (the reference's main over the C ABI) exits 0 and

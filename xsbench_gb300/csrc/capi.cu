@@ -209,6 +209,7 @@ void xs_ctx_destroy(xs_ctx *ctx)
     if (ctx->pipe_buf) cudaFree(ctx->pipe_buf);
     if (ctx->s.plain_buf) cudaFree(ctx->s.plain_buf);
     if (ctx->s.adj_buf) cudaFree(ctx->s.adj_buf);
+    if (ctx->s.hist_buf) cudaFree(ctx->s.hist_buf);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -720,7 +721,10 @@ xs_status xs_run_history(xs_ctx *ctx, const xs_run_opts *opts, xs_run_result *re
     XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, st));
     XS_CUDA(cudaEventRecord(ctx->ev0, st));
     int launches = 0;
-    s = launch_history(ctx, st, o.arith, o.first, o.count, &launches);
+    s = o.kernel == XS_KERNEL_BATCHED
+            ? launch_history_stepped(ctx, st, o.arith, o.first, o.count,
+                                     opts && opts->tile_lookups > 0 ? opts->tile_lookups : 0, &launches)
+            : launch_history(ctx, st, o.arith, o.first, o.count, &launches);
     if (s != XS_OK) return s;
     XS_CUDA(cudaEventRecord(ctx->ev1, st));
     s = read_back(ctx, st, result);

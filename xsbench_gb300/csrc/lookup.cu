@@ -11,6 +11,8 @@
 #include <cstdio>
 #include <cstring>
 
+#include <algorithm>
+
 #include "lookup_kernels.cuh"
 
 namespace xsgb {
@@ -502,6 +504,92 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
     }
     XS_CUDA(cudaGraphLaunch(it->second.exec, st));
     if (launches) *launches += it->second.launches;
+    return XS_OK;
+}
+
+// Stepped history: particle p's state (seed, energy, material) before its
+// first lookup (Simulation.c:160-175; the skip is multiplied in int there).
+__global__ void k_history_init(Tables t, long first, long count, int nl,
+                               unsigned long long *seed, double *E, int *mat)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long)gridDim.x * blockDim.x) {
+        const long p = first + i;
+        const int skip = (int)((unsigned)(int)p * (unsigned)nl * 2u * 5u);
+        unsigned long long s = lcg_skip(kStartingSeed, (unsigned long long)(long long)skip);
+        E[i] = lcg_next(s);
+        mat[i] = pick_mat(t, s);
+        seed[i] = s;
+    }
+}
+
+// The state after a lookup (Simulation.c:205-224): one skip per macro_xs
+// channel above 1.0, then the next energy and material.
+__global__ void k_history_advance(Tables t, long count, const double *macro,
+                                  unsigned long long *seed, double *E, int *mat)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long)gridDim.x * blockDim.x) {
+        unsigned long long nf = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) nf += macro[i * 5 + k] > 1.0;
+        unsigned long long s = seed[i];
+        if (nf) s = lcg_skip(s, nf);
+        E[i] = lcg_next(s);
+        mat[i] = pick_mat(t, s);
+        seed[i] = s;
+    }
+}
+
+xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                                 int tile, int *launches)
+{
+    const int nl = ctx->inputs.lookups;
+    if (tile <= 0) tile = 256;   // a step is one batch of `count` lookups: small tiles fill the GPU
+    const size_t ps_bytes = plain_scratch_bytes(count, tile);
+    const size_t need = (size_t)count * (8 + 8 + 4 + 40) + ps_bytes + 4096;
+    if (ctx->s.hist_bytes < need) {
+        if (ctx->s.hist_buf) {
+            cudaFree(ctx->s.hist_buf);
+            ctx->device_bytes -= ctx->s.hist_bytes;
+            ctx->s.hist_buf = nullptr;
+            ctx->s.hist_bytes = 0;
+        }
+        cudaError_t e = cudaMalloc(&ctx->s.hist_buf, need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(XS_ERR_OUT_OF_MEMORY, "history particle states (%zu bytes)", need);
+        }
+        ctx->s.hist_bytes = need;
+        ctx->device_bytes += need;
+    }
+    char *b = (char *)ctx->s.hist_buf;
+    auto take = [&](size_t bytes) { char *r = b; b += (bytes + 255) & ~(size_t)255; return r; };
+    unsigned long long *seed = (unsigned long long *)take((size_t)count * 8);
+    double *E = (double *)take((size_t)count * 8);
+    int *mat = (int *)take((size_t)count * 4);
+    double *macro = (double *)take((size_t)count * 40);
+    PlainScratch ps = carve_plain_scratch(take(ps_bytes), count, tile);
+    const bool ovf = count > 8L * tile && ctx->t.grid_type != XS_NUCLIDE;
+    const unsigned blocks = (unsigned)std::min<long>((count + 255) / 256, (long)ctx->sm_count * 16);
+    k_history_init<<<blocks, 256, 0, st>>>(ctx->t, first, count, nl, seed, E, mat);
+    XS_CUDA(cudaGetLastError());
+    int n = 1;
+    SampleInput in;
+    in.energy = E;
+    in.mat = mat;
+    Outputs out;
+    out.macro = macro;
+    for (int step = 0; step < nl; step++) {
+        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, in, out, ovf ? &ps : nullptr, &n);
+        if (s != XS_OK) return s;
+        if (step + 1 < nl) {
+            k_history_advance<<<blocks, 256, 0, st>>>(ctx->t, count, macro, seed, E, mat);
+            XS_CUDA(cudaGetLastError());
+            n++;
+        }
+    }
+    if (launches) *launches += n;
     return XS_OK;
 }
 

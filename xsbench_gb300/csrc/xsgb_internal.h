@@ -73,6 +73,8 @@ struct Scratch {
     size_t plain_bytes = 0;
     void *adj_buf = nullptr;                     // adjoint sort, tables and partials
     size_t adj_bytes = 0;
+    void *hist_buf = nullptr;                    // stepped history: particle states
+    size_t hist_bytes = 0;
 };
 
 struct BatchedGraph {
@@ -168,6 +170,9 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
                          const Outputs &out, int *launches);
 xs_status launch_history(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
                          int *launches);
+// History mode advanced in lockstep: one event batch per lookup step.
+xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
+                                 int tile, int *launches);
 size_t batched_scratch_bytes(long count, int buckets);
 // Explicit device buffers of one batched run (every pointer into caller memory).
 struct BatchedScratch {
