@@ -263,6 +263,46 @@ def test_c_driver_reports_the_published_hash(args, expect):
     assert str(expect) in out.stdout
 
 
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_nuclide", "tiny_hash"])
+@pytest.mark.parametrize("kernel", ["plain", "batched"])
+@pytest.mark.parametrize("arith", ["fast", "exact"])
+def test_edge_energies_against_oracle(name, kernel, arith):
+    """Caller samples at the edges the searches must get right: zero and
+    subnormal energies, energies equal to gridpoints, the hash grid's bin
+    edges and the doubles just below them, 1 - 2^-53; on the unionized and
+    nuclide grids also energies outside [0, 1) and NaN (on the hash grid the
+    reference indexes outside its table for those, Simulation.c:350).  The
+    argmax vector and the verification sum bit-exact; macro_xs bit-identical
+    (EXACT) or within REL_TOL (FAST), NaN where the reference gives NaN."""
+    rng = np.random.default_rng(11)
+    with oracle.Problem(oracle_config(name)) as o:
+        grid = np.array(o.arrays()["nuclide_grid"]).reshape(-1, 6)[:, 0]
+        edges = np.arange(500) / 500.0
+        E = [np.array([0.0, 5e-324, 1e-300, 1.0 - 2.0 ** -53]),
+             grid[rng.integers(0, grid.size, 3000)],
+             edges, np.nextafter(edges[1:], 0.0),
+             rng.random(2000)]
+        if name != "tiny_hash":
+            E.append(np.array([1.0, 1.5, -0.25, 1e10, -1e10, np.nan, np.inf]))
+        E = np.concatenate(E)
+        M = rng.integers(0, 12, E.size).astype(np.int32)
+        ref = o.run_samples(E, M)
+    ctx = ctx_for(name)
+    macro = np.empty((E.size, 5))
+    idx = np.empty(E.size, np.uint8)
+    r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel=kernel, arith=arith)
+    assert r.verification == ref["verification"]
+    assert np.array_equal(idx, ref["max_idx"])
+    fin = np.isfinite(ref["macro"])
+    assert np.array_equal(np.isfinite(macro), fin)
+    assert np.array_equal(macro[~fin], ref["macro"][~fin], equal_nan=True)   # same inf / NaN
+    if arith == "exact":
+        assert np.array_equal(macro[fin], ref["macro"][fin])
+    else:
+        rows = fin.all(axis=1)
+        assert rel_err(macro[rows], ref["macro"][rows]) <= REL_TOL
+
+
 def test_drop_in_seam():
     g = golden_json("full_tiny_unionized")
     inp = product_inputs("tiny_unionized")
