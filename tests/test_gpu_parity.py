@@ -245,17 +245,15 @@ def test_history_full_published_hash(size):
                 assert r.verification % 999983 == g["hash"]
 
 
-@pytest.mark.parametrize("args,expect", [
-    (["-m", "event", "-s", "small", "-k", "0"], 945990),
-    (["-m", "event", "-s", "small", "-k", "1"], 945990),
-    (["-m", "event", "-s", "small", "-k", "2"], 945990),
-    (["-m", "event", "-s", "small", "-G", "hash", "-k", "3"], 945990),
-    (["-m", "history", "-s", "small"], 941535),
-    (["-m", "history", "-s", "small", "-k", "1"], 941535),
-])
-def test_c_driver_reports_the_published_hash(args, expect):
-    """The C host program (the reference's main over the C ABI) exits 0 and
-    prints the reference's verification value."""
+@pytest.mark.parametrize("method,expect", [("event", 945990), ("history", 941535)])
+@pytest.mark.parametrize("grid", ["unionized", "nuclide", "hash"])
+@pytest.mark.parametrize("kid", ["0", "1", "2", "3"])
+def test_c_driver_reports_the_published_hash(method, expect, grid, kid):
+    """The reference's CI matrix (.travis.yml:21-28: history / event x the three
+    grid types, small problem) through the C host program (the reference's main
+    over the C ABI), for every kernel id: exit status 0 and the published
+    verification value (io.c:89-95)."""
+    args = ["-m", method, "-s", "small", "-G", grid, "-k", kid]
     import subprocess
     from xsbench_gb300 import build as B
     out = subprocess.run([B.EXE_PATH, *args], capture_output=True, text=True, timeout=600)
