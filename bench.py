@@ -395,6 +395,8 @@ def main():
 
     line = None
     if rank == 0:
+        sm_mhz = (clk or {}).get("sm_max_mhz") or 2070.0
+        fp64_peak = 2.0 * torch.cuda.get_device_properties(local).multi_processor_count * sm_mhz * 1e6
         bpl = algorithmic_bytes_per_lookup(inputs, list(problem.arrays()["num_nucs"]))
         peak, peak_kind = measured_peak_gbs()
         per_launch_s = t / args.steps
@@ -427,12 +429,13 @@ def main():
                          "traffic_source": traffic_src},
             # the other bound of this FP64 path: 11 FP64 instructions per nuclide
             # (FAST records: one subtraction, five interpolations, five
-            # accumulations) against GB300's FP64 rate (1.25 TFLOP/s nominal =
-            # 625 G fused multiply-adds per second)
+            # accumulations) against the FP64 pipe's rate, 2 per SM per clock
+            # (ncu's peak_sustained for DFMA) x SMs x the maximum SM clock
             "fp64": ({"ops_per_lookup": round(11 * nbar_of(inputs, problem), 1),
                       "achieved_gops": value * 11 * nbar_of(inputs, problem) / 1e9,
-                      "peak_gops": 625.0, "peak_source": "nominal GB300 FP64 FMA rate",
-                      "frac": value * 11 * nbar_of(inputs, problem) / 625e9}
+                      "peak_gops": fp64_peak / 1e9,
+                      "peak_source": "2 FP64 ops per SM per clock x SMs x max SM clock",
+                      "frac": value * 11 * nbar_of(inputs, problem) / fp64_peak}
                      if args.arith == "fast" and args.kernel == "plain" else None),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 12,
                     "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",

@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "xsgb.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(xs_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(xs_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_every_declared_symbol_is_exported():
