@@ -394,6 +394,7 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->fuel_lanes = v;
     }
+    if (const char *env = getenv("XSGB_STAGE_ROWS")) ctx->stage_rows = atoi(env) != 0 ? 1 : 0;
     if (const char *env = getenv("XSGB_BATCHED_FUEL_LANES")) {
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->batched_fuel_lanes = v;

@@ -77,6 +77,23 @@ __device__ __forceinline__ T ldg(const T *p)
     return __ldg(p);
 }
 
+// A material row entry: from shared memory (S, rows staged by the block) or
+// through the read-only cache.
+template <bool S, typename T>
+__device__ __forceinline__ T rd(const T *p)
+{
+    if constexpr (S) return *p;
+    else return __ldg(p);
+}
+
+// The materials' nuclide lists and concentrations staged in shared memory:
+// material m's row is mats[off[m] .. off[m+1]), concs likewise.
+struct SRows {
+    const int *mats = nullptr;
+    const double *concs = nullptr;
+    const int *off = nullptr;
+};
+
 // Error reporting from checked kernels: first error wins.
 __device__ __forceinline__ void report(int *err, int code, long a, long b)
 {
@@ -426,7 +443,7 @@ __device__ __forceinline__ const void *interval_bytes(const Tables &t, int nuc, 
 //
 // TABLE (FAST arithmetic, union table built): the lane reads its nuclides'
 // entries of the row instead of index entries and interval records.
-template <int ARITH, bool CHECKED, bool DE, bool TABLE = false>
+template <int ARITH, bool CHECKED, bool DE, bool TABLE = false, bool SROW = false>
 __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, int mat, int n,
                                                    const int *mrow, const double *crow,
                                                    double macro[5], int *err, double *S,
@@ -445,7 +462,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             const double2 *p = blk + (long)j * 5;
             const double2 a0 = ld_v2(p, pol), a1 = ld_v2(p + 1, pol), a2 = ld_v2(p + 2, pol);
             const double2 a3 = ld_v2(p + 3, pol), a4 = ld_v2(p + 4, pol);
-            const double conc = ldg(&crow[j]);
+            const double conc = rd<SROW>(&crow[j]);
             macro[0] = fma(fma(a0.y, dl, a0.x), conc, macro[0]);
             macro[1] = fma(fma(a1.y, dl, a1.x), conc, macro[1]);
             macro[2] = fma(fma(a2.y, dl, a2.x), conc, macro[2]);
@@ -476,13 +493,13 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
     const long top = t.n_gp - 1;
     int kr[2 * P];
 #pragma unroll
-    for (int q = 0; q < 2 * P; q++) kr[q] = (q < nl) ? ldg(&irow[ldg(&mrow[q * stride])]) : 0;
+    for (int q = 0; q < 2 * P; q++) kr[q] = (q < nl) ? ldg(&irow[rd<SROW>(&mrow[q * stride])]) : 0;
 #pragma unroll
     for (int q = 0; q < P; q++)
         if (q < nl) {
             long k = kr[q];
             if (CHECKED && (k < 0 || k > top)) k = 0;
-            const int nq = ldg(&mrow[q * stride]);
+            const int nq = rd<SROW>(&mrow[q * stride]);
             prefetch_l2(interval_bytes<ARITH>(t, nq, k == top ? k - 1 : k), 96, prefetch_policy(t, nq));
         }
     for (int j0 = 0; j0 < nl; j0 += 2 * P) {
@@ -492,22 +509,22 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             if (j < nl) {
                 long k = kr[q];
                 if (CHECKED && (k < 0 || k > top)) {
-                    report(err, XS_ERR_DATA, row, ldg(&mrow[j * stride]));
+                    report(err, XS_ERR_DATA, row, rd<SROW>(&mrow[j * stride]));
                     k = 0;
                 }
                 if (k == top) k -= 1;
                 const int jn = j + 2 * P;
-                if (jn < nl) kr[q] = ldg(&irow[ldg(&mrow[jn * stride])]);
+                if (jn < nl) kr[q] = ldg(&irow[rd<SROW>(&mrow[jn * stride])]);
                 const int jp = j + P;
                 if (jp < nl) {
                     long kp = kr[(q + P) % (2 * P)];
                     if (CHECKED && (kp < 0 || kp > top)) kp = 0;
-                    const int np = ldg(&mrow[jp * stride]);
+                    const int np = rd<SROW>(&mrow[jp * stride]);
                     prefetch_l2(interval_bytes<ARITH>(t, np, kp == top ? kp - 1 : kp), 96,
                                 prefetch_policy(t, np));
                 }
-                const int nuc = ldg(&mrow[j * stride]);
-                const double conc = ldg(&crow[j * stride]);
+                const int nuc = rd<SROW>(&mrow[j * stride]);
+                const double conc = rd<SROW>(&crow[j * stride]);
                 if (ARITH == XS_ARITH_EXACT)
                     accumulate_exact(t, nuc, k, E, conc, macro);
                 else
@@ -581,10 +598,12 @@ __device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E,
 // With DE, S[5] receives d macro_xs / dE (the adjoint's energy derivative).
 // With stride > 1 the call computes the partial sum over the nuclides
 // j = q0, q0 + stride, ... only (one of `stride` lanes sharing the lookup).
-template <int GRID, int ARITH, bool CHECKED, bool DE = false, bool TABLE = false>
+//
+// SROW: the material's row is read from the block's staged copy `sr`.
+template <int GRID, int ARITH, bool CHECKED, bool DE = false, bool TABLE = false, bool SROW = false>
 __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, double macro[5],
                                          int *err, double *S = nullptr, int q0 = 0,
-                                         int stride = 1)
+                                         int stride = 1, SRows sr = SRows())
 {
 #pragma unroll
     for (int c = 0; c < 5; c++) macro[c] = 0.0;
@@ -592,12 +611,22 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
 #pragma unroll
         for (int c = 0; c < 5; c++) S[c] = 0.0;
     }
-    const int n = ldg(&t.num_nucs[mat]);
-    const int *mrow = t.mats + mat * t.max_nucs;
-    const double *crow = t.concs + mat * t.max_nucs;
+    int n;
+    const int *mrow;
+    const double *crow;
+    if constexpr (SROW) {
+        const int o = sr.off[mat];
+        n = sr.off[mat + 1] - o;
+        mrow = sr.mats + o;
+        crow = sr.concs + o;
+    } else {
+        n = ldg(&t.num_nucs[mat]);
+        mrow = t.mats + mat * t.max_nucs;
+        crow = t.concs + mat * t.max_nucs;
+    }
     if (GRID == XS_UNIONIZED) {
-        macro_xs_unionized<ARITH, CHECKED, DE, TABLE>(t, E, mat, n, mrow, crow, macro, err, S, q0,
-                                                      stride);
+        macro_xs_unionized<ARITH, CHECKED, DE, TABLE, SROW>(t, E, mat, n, mrow, crow, macro, err,
+                                                            S, q0, stride);
         return;
     }
     long row = 0;
@@ -618,8 +647,8 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
     }
 #pragma unroll 2
     for (int j = q0; j < n; j += stride) {
-        const int nuc = ldg(&mrow[j]);
-        const double conc = ldg(&crow[j]);
+        const int nuc = rd<SROW>(&mrow[j]);
+        const double conc = rd<SROW>(&crow[j]);
         long k;
         if (GRID == XS_UNIONIZED) {
             k = interval_unionized<CHECKED>(t, row, nuc, err);

@@ -248,6 +248,9 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
     a.ovf_id = ps ? ps->id : nullptr;
     a.ovf_cap = ps ? ps->cap : 0;
     a.fuel_lanes = ctx->fuel_lanes;
+    a.stage_rows = ctx->stage_rows >= 0 ? ctx->stage_rows : ctx->t.grid_type == XS_UNIONIZED;
+    a.rows_total = 0;
+    for (int m = 0; m < kMaterials; m++) a.rows_total += ctx->num_nucs_host[m];
     if (ps) {
         XS_CUDA(cudaMemsetAsync(ps->cnt, 0, 256, st));  // counts, layout, queue
     }

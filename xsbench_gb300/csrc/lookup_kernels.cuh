@@ -35,6 +35,10 @@ struct PlainArgs {
     // added in a fixed tree), so a fuel chunk is 32 / fuel_lanes lookups and
     // the block's warps finish their tile together
     int fuel_lanes;
+    // 1: the block stages every material's nuclide list and concentrations
+    // (rows_total entries in all) in shared memory
+    int stage_rows;
+    int rows_total;
 };
 
 // A material-segmented list of lookups (the batched sort, or the plain
@@ -93,13 +97,13 @@ __device__ __forceinline__ bool sample_at(const Tables &t, const double *in_E, c
 }
 
 // One lookup of the event batch: macro_xs, argmax, outputs.
-template <int GRID, int ARITH, bool CHECKED, bool TABLE>
+template <int GRID, int ARITH, bool CHECKED, bool TABLE, bool SROW = false>
 __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, int m, long o,
                                                      double *out_macro, unsigned char *out_idx,
-                                                     int *err)
+                                                     int *err, SRows sr = SRows())
 {
     double macro[5];
-    macro_xs<GRID, ARITH, CHECKED, false, TABLE>(t, E, m, macro, err);
+    macro_xs<GRID, ARITH, CHECKED, false, TABLE, SROW>(t, E, m, macro, err, nullptr, 0, 1, sr);
     const int arg = argmax5(macro);
     if (out_macro) {
 #pragma unroll
@@ -114,14 +118,17 @@ __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, 
 // tree (q0 + q1) + (q2 + q3), which gives the same bits on every lane of the
 // lookup.  Every lane of the warp calls this (shuffles); `live` is the same on
 // the L lanes of a lookup.  Returns argmax+1 on the lookup's lane q == 0.
-template <int GRID, bool CHECKED, bool TABLE>
+template <int GRID, bool CHECKED, bool TABLE, bool SROW = false>
 __device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool live, double E,
                                                            long o, int q, int L,
                                                            double *out_macro,
-                                                           unsigned char *out_idx, int *err)
+                                                           unsigned char *out_idx, int *err,
+                                                           SRows sr = SRows())
 {
     double macro[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    if (live) macro_xs<GRID, XS_ARITH_FAST, CHECKED, false, TABLE>(t, E, 0, macro, err, nullptr, q, L);
+    if (live)
+        macro_xs<GRID, XS_ARITH_FAST, CHECKED, false, TABLE, SROW>(t, E, 0, macro, err, nullptr, q,
+                                                                   L, sr);
     for (int s = 1; s < L; s <<= 1) {
 #pragma unroll
         for (int k = 0; k < 5; k++) macro[k] += __shfl_xor_sync(0xffffffffu, macro[k], s);
@@ -188,7 +195,7 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
 // different row of a table of ~155 GB, and the page-translation misses of that
 // pattern cost more than the bytes it saves (the batched kernel, whose warps
 // read neighbouring rows, uses it).
-template <int GRID, int ARITH, bool CHECKED, bool SAMPLES>
+template <int GRID, int ARITH, bool CHECKED, bool SAMPLES, bool SROW = false>
 __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables t, PlainArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -197,8 +204,35 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
     int *perm = reinterpret_cast<int *>(sE + tile);
     unsigned char *sMat = reinterpret_cast<unsigned char *>(perm + tile + kMaterials * 32);
     __shared__ int cnt[kMaterials], cur[kMaterials], seg[kMaterials + 1], obase[kMaterials];
+    __shared__ int roff[kMaterials + 1];
     __shared__ unsigned int qhead;
     __shared__ unsigned long long s_acc;
+    SRows sr;
+    if constexpr (SROW) {
+        // after the tile's arrays, 8-byte aligned: concs, then nuclide ids
+        const size_t o = ((size_t)tile * 13 + kMaterials * 128 + 7) & ~(size_t)7;
+        double *sc = reinterpret_cast<double *>(smem + o);
+        int *sm = reinterpret_cast<int *>(sc + a.rows_total);
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int m = 0; m < kMaterials; m++) {
+                roff[m] = s;
+                s += ldg(&t.num_nucs[m]);
+            }
+            roff[kMaterials] = s;
+        }
+        __syncthreads();
+        for (int m = 0; m < kMaterials; m++) {
+            const int o0 = roff[m], n = roff[m + 1] - o0;
+            for (int j = threadIdx.x; j < n; j += kBlock) {
+                sc[o0 + j] = ldg(&t.concs[m * t.max_nucs + j]);
+                sm[o0 + j] = ldg(&t.mats[m * t.max_nucs + j]);
+            }
+        }
+        sr.mats = sm;
+        sr.concs = sc;
+        sr.off = roff;
+    }
 
     const int tid = threadIdx.x;
     const long base = (long)blockIdx.x * tile;
@@ -290,8 +324,8 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
             const int p = (int)c * (32 / L) + lane / L;
             const bool live = p < (overflow ? (cnt[0] & ~31) : cnt[0]);
             const int l = live ? perm[p] : 0;
-            mine += split_lookup_and_store<GRID, CHECKED, false>(t, live, sE[l], base + l, q, L,
-                                                                 a.out_macro, a.out_idx, a.err);
+            mine += split_lookup_and_store<GRID, CHECKED, false, SROW>(
+                t, live, sE[l], base + l, q, L, a.out_macro, a.out_idx, a.err, sr);
             continue;
         }
         const int cv = (int)c - nfuel + (fuel_v >> 5);
@@ -301,8 +335,8 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
         const int limit = seg[m] + (overflow ? (cnt[m] & ~31) : cnt[m]);
         if (p < limit) {
             const int l = perm[p];
-            mine += lookup_and_store<GRID, ARITH, CHECKED, false>(t, sE[l], m, base + l, a.out_macro,
-                                                                  a.out_idx, a.err);
+            mine += lookup_and_store<GRID, ARITH, CHECKED, false, SROW>(
+                t, sE[l], m, base + l, a.out_macro, a.out_idx, a.err, sr);
         }
     }
     block_verification(mine, &s_acc, a.verif);
@@ -467,9 +501,10 @@ __global__ void __launch_bounds__(kBlock) k_history(Tables t, long first, long c
 }
 
 // ------------------------------------------------------------ launchers ---
-inline size_t plain_smem_bytes(int tile)
+inline size_t plain_smem_bytes(int tile, int rows_total = 0)
 {
-    return (size_t)tile * 8 + (size_t)(tile + kMaterials * 32) * 4 + tile;
+    const size_t b = (size_t)tile * 8 + (size_t)(tile + kMaterials * 32) * 4 + tile;
+    return rows_total ? ((b + 7) & ~(size_t)7) + (size_t)rows_total * 12 : b;
 }
 
 template <int GRID>
@@ -478,18 +513,30 @@ struct GridLaunch {
                              bool samples, const PlainArgs &a)
     {
         const long blocks = (a.count + a.tile - 1) / a.tile;
-        const size_t sm = plain_smem_bytes(a.tile);
-#define XSGB_PLAIN(A, C, S)                                                                   \
+        const bool srow = a.stage_rows && a.rows_total > 0 &&
+                          plain_smem_bytes(a.tile, a.rows_total) <= 96 * 1024;
+        const size_t sm = plain_smem_bytes(a.tile, srow ? a.rows_total : 0);
+        // shared-memory share of the SM's 228 KB that holds the resident
+        // blocks (each with its static arrays and 1 KB reserved), L1 the rest
+        const int carve = srow ? (int)((XSGB_PLAIN_MIN_BLOCKS * (sm + 1280) * 100 + 233471) / 233472)
+                               : 25;
+#define XSGB_PLAIN_R(A, C, S, R)                                                              \
     do {                                                                                      \
-        auto k = k_plain<GRID, A, C, S>;                                                      \
+        auto k = k_plain<GRID, A, C, S, R>;                                                   \
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                              (int)sm);                                        \
         if (e == cudaSuccess)                                                                 \
-            e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 25);  \
+            e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,       \
+                                     carve < 100 ? carve : 100);                              \
         if (e != cudaSuccess) return e;                                                       \
         k<<<(unsigned)blocks, kBlock, sm, st>>>(t, a);                                        \
         return cudaGetLastError();                                                            \
     } while (0)
+#define XSGB_PLAIN(A, C, S) XSGB_PLAIN_R(A, C, S, false)
+        if (srow && !checked && arith != XS_ARITH_EXACT) {
+            if (samples) XSGB_PLAIN_R(XS_ARITH_FAST, false, true, true);
+            XSGB_PLAIN_R(XS_ARITH_FAST, false, false, true);
+        }
         if (checked) {
             if (samples) XSGB_PLAIN(XS_ARITH_FAST, true, true);
             XSGB_PLAIN(XS_ARITH_FAST, true, false);
@@ -501,6 +548,7 @@ struct GridLaunch {
         if (samples) XSGB_PLAIN(XS_ARITH_FAST, false, true);
         XSGB_PLAIN(XS_ARITH_FAST, false, false);
 #undef XSGB_PLAIN
+#undef XSGB_PLAIN_R
     }
 
     static cudaError_t list(const Tables &t, cudaStream_t st, int arith, int checked, int blocks,
