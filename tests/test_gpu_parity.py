@@ -104,6 +104,30 @@ def test_fuel_lane_split(monkeypatch, name, lanes, table):
             assert rel_err(macro, ref) <= REL_TOL, kernel
 
 
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "tiny_nuclide"])
+def test_staged_material_rows(monkeypatch, name):
+    """The plain kernel reading the materials' nuclide lists and concentrations
+    from shared memory (staged by each block) or through the read-only cache:
+    bit-identical macro_xs either way and the reference's hash, with the
+    overflow pass (200,000 lookups) and without it (4,096 lookups)."""
+    g = golden_json("full_" + name)
+    got = {}
+    for stage in ("0", "1"):
+        monkeypatch.setenv("XSGB_STAGE_ROWS", stage)
+        for n in (g["lookups"], 4096):
+            inp = product_inputs(name, lookups=n)
+            with X.grid_init(inp) as prob, X.Context(inp, prob) as ctx:
+                for arith in ("fast", "exact"):
+                    r, macro, _ = run(ctx, n, kernel="plain", arith=arith)
+                    if n == g["lookups"]:
+                        assert r.verification == g["verification"], (stage, arith)
+                    got[stage, arith, n] = (r.verification, macro)
+    for key in [k[1:] for k in got if k[0] == "0"]:
+        v0, m0 = got[("0",) + key]
+        v1, m1 = got[("1",) + key]
+        assert v0 == v1 and np.array_equal(m0, m1), key
+
+
 @pytest.mark.parametrize("name", ["small_unionized", "small_hash", "small_nuclide",
                                   "large_unionized", "large_hash", "large_nuclide"])
 def test_full_size_against_reference(name):
