@@ -45,35 +45,155 @@ __device__ __forceinline__ bool pair_less(long long ka, int ia, long long kb, in
 }
 
 // ---------------------------------------------------------- bucket sort ---
+constexpr int kSubRun = 32;            // longest sub-bucket sorted by insertion
+
+// Sub-bucket of order key k among nsub equal key ranges of [kmin, kmax]: a
+// non-decreasing function of k (the conversion to double, the product with a
+// positive scale and the truncation are each monotone).
+__device__ __forceinline__ int sub_of(long long k, long long kmin, double scale, int nsub)
+{
+    const int s = (int)((double)((unsigned long long)k - (unsigned long long)kmin) * scale);
+    return s < nsub - 1 ? s : nsub - 1;
+}
+
+// Block-wide min and max (256 threads); every thread gets the results.
+__device__ __forceinline__ void block_minmax(long long &lo, long long &hi, long long *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long a = __shfl_xor_sync(0xffffffffu, lo, o), b = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[w] = lo;
+        red[8 + w] = hi;
+    }
+    __syncthreads();
+    lo = red[0];
+    hi = red[8];
+    for (int i = 1; i < 8; i++) {
+        lo = red[i] < lo ? red[i] : lo;
+        hi = red[8 + i] > hi ? red[8 + i] : hi;
+    }
+    __syncthreads();
+}
+
+// Exclusive scan of c[0, n) in place, n <= 1024 (256 threads, four each).
+__device__ __forceinline__ void block_scan_1024(int *c, int n, long long *red)
+{
+    const int t = threadIdx.x;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        v[q] = (4 * t + q < n) ? c[4 * t + q] : 0;
+        sum += v[q];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, inc, o);
+        if ((t & 31) >= o) inc += x;
+    }
+    int *wsum = reinterpret_cast<int *>(red);
+    if ((t & 31) == 31) wsum[t >> 5] = inc;
+    __syncthreads();
+    int base = 0;
+    for (int i = 0; i < (t >> 5); i++) base += wsum[i];
+    int run = base + inc - sum;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (4 * t + q < n) c[4 * t + q] = run;
+        run += v[q];
+    }
+    __syncthreads();
+}
+
 // One block per bucket: sort the bucket's (energy, id) entries by (order key
-// of the energy, id).  Buckets up to kSortCap entries sort in shared memory;
-// larger ones in place in global memory.  Both use the bitonic network in its
-// all-ascending form (first step of each merge pairs i with i ^ (k-1)), so
-// positions past the bucket act as +infinity and never move.
+// of the energy, id).  A bucket of up to kSortCap entries is loaded into
+// shared memory and spread over n/2 sub-buckets, equal ranges of its keys
+// (the keys of one bucket are close to uniform): a counting pass, a scan,
+// a scatter of entry indices, then each thread sorts one sub-bucket (about
+// two entries) by insertion on (key, id).  The order is the unique (key, id)
+// order whatever the scatter's arrival order, so the result is deterministic.
+// A bucket whose keys crowd one sub-bucket (more than kSubRun entries, e.g.
+// repeated energies) takes the bitonic network in shared memory instead, and
+// a bucket larger than kSortCap the same network in place in global memory;
+// both use its all-ascending form (first step of each merge pairs i with
+// i ^ (k-1)), so positions past the bucket act as +infinity and never move.
+// Dynamic shared memory: bucket_sort_smem_bytes().
 __global__ void __launch_bounds__(256) k_bucket_sort(const int *starts, const int *ends,
                                                      int nbuckets, double *sE, int *sid)
 {
-    __shared__ long long key[kSortCap];
-    __shared__ int id[kSortCap];
-    __shared__ double ev[kSortCap];
+    extern __shared__ __align__(16) unsigned char bsm[];
+    long long *key = reinterpret_cast<long long *>(bsm);
+    double *ev = reinterpret_cast<double *>(key + kSortCap);
+    int *id = reinterpret_cast<int *>(ev + kSortCap);
+    int *cur = id + kSortCap;                                            // [kSortCap / 2]
+    unsigned short *perm = reinterpret_cast<unsigned short *>(cur + kSortCap / 2);
+    __shared__ long long red[16];
     for (int b = blockIdx.x; b < nbuckets; b += gridDim.x) {
         const int a = starts[b], n = ends[b] - a;
         if (n <= 1) continue;
         int P = 1;
         while (P < n) P <<= 1;
         if (n <= kSortCap) {
+            long long lo = 0x7FFFFFFFFFFFFFFFLL, hi = -0x7FFFFFFFFFFFFFFFLL - 1;
             for (int i = threadIdx.x; i < P; i += blockDim.x) {
                 if (i < n) {
                     ev[i] = sE[a + i];
                     key[i] = order_key(ev[i]);
                     id[i] = sid[a + i];
+                    lo = key[i] < lo ? key[i] : lo;
+                    hi = key[i] > hi ? key[i] : hi;
                 } else {
                     key[i] = 0x7FFFFFFFFFFFFFFFLL;
                     id[i] = 0x7FFFFFFF;
                     ev[i] = 0.0;
                 }
             }
+            block_minmax(lo, hi, red);   // (its barriers also publish the loads)
+            const int nsub = n >> 1;
+            const double scale =
+                (double)nsub / ((double)((unsigned long long)hi - (unsigned long long)lo) + 1.0);
+            for (int s = threadIdx.x; s < nsub; s += blockDim.x) cur[s] = 0;
             __syncthreads();
+            for (int i = threadIdx.x; i < n; i += blockDim.x)
+                atomicAdd(&cur[sub_of(key[i], lo, scale, nsub)], 1);
+            __syncthreads();
+            long long most = 0, unused = 0;
+            for (int s = threadIdx.x; s < nsub; s += blockDim.x) most = cur[s] > most ? cur[s] : most;
+            block_minmax(unused, most, red);
+            if (most <= kSubRun) {
+                block_scan_1024(cur, nsub, red);
+                for (int i = threadIdx.x; i < n; i += blockDim.x)
+                    perm[atomicAdd(&cur[sub_of(key[i], lo, scale, nsub)], 1)] = (unsigned short)i;
+                __syncthreads();
+                // cur[s] is now the end of sub-bucket s
+                for (int s = threadIdx.x; s < nsub; s += blockDim.x) {
+                    const int s0 = s ? cur[s - 1] : 0, s1 = cur[s];
+                    for (int i = s0 + 1; i < s1; i++) {
+                        const unsigned short x = perm[i];
+                        const long long kx = key[x];
+                        const int ix = id[x];
+                        int j = i - 1;
+                        while (j >= s0 && pair_less(kx, ix, key[perm[j]], id[perm[j]])) {
+                            perm[j + 1] = perm[j];
+                            j--;
+                        }
+                        perm[j + 1] = x;
+                    }
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    const int x = perm[i];
+                    sE[a + i] = ev[x];
+                    sid[a + i] = id[x];
+                }
+                __syncthreads();
+                continue;
+            }
             for (int k = 2; k <= P; k <<= 1) {
                 for (int j = k >> 1; j > 0; j >>= 1) {
                     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -112,6 +232,22 @@ __global__ void __launch_bounds__(256) k_bucket_sort(const int *starts, const in
             }
         }
     }
+}
+
+size_t bucket_sort_smem_bytes()
+{
+    return (size_t)kSortCap * (8 + 8 + 4 + 2) + (size_t)(kSortCap / 2) * 4;
+}
+
+cudaError_t launch_bucket_sort(const int *starts, const int *ends, int nbuckets, double *sE,
+                               int *sid, int blocks, cudaStream_t st)
+{
+    const size_t sm = bucket_sort_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(k_bucket_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm);
+    if (e != cudaSuccess) return e;
+    k_bucket_sort<<<blocks, 256, sm, st>>>(starts, ends, nbuckets, sE, sid);
+    return cudaGetLastError();
 }
 
 // gradients into sorted order (zeros on padding positions)
@@ -564,8 +700,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
                                     cnt, sE, sid);
     if (s != XS_OK) return s;
     const int nbuckets = kMaterials * nb;
-    k_bucket_sort<<<std::min(nbuckets, ctx->sm_count * 8), 256, 0, st>>>(starts, offs, nbuckets, sE, sid);
-    XS_CUDA(cudaGetLastError());
+    XS_CUDA(launch_bucket_sort(starts, offs, nbuckets, sE, sid, std::min(nbuckets, ctx->sm_count * 8), st));
     k_gather_gbar<<<ctx->sm_count * 8, 256, 0, st>>>(seg, cnt, sid, gbar, sg);
     XS_CUDA(cudaGetLastError());
 

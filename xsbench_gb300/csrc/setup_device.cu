@@ -23,7 +23,6 @@
 
 namespace xsgb {
 
-__global__ void k_bucket_sort(const int *starts, const int *ends, int nbuckets, double *sE, int *sid);
 __global__ void k_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, double du,
                             int *index);
 
@@ -233,8 +232,9 @@ static xs_status segmented_sort(xs_ctx *ctx, cudaStream_t st, const double *vals
         k_iscan_local<<<std::min<long>(nblk, sm * 8), kIScan, 0, st>>>(offs, nkeys, bsum);
         k_bucket_pass<true><<<sm * 16, 256, 0, st>>>(vals, stride, n, seg_len, nb, offs, outE, outId);
         k_bucket_starts<<<sm * 8, 256, 0, st>>>(offs, counts, nkeys, starts);
-        k_bucket_sort<<<std::min<long>(nkeys, (long)sm * 16), 256, 0, st>>>(starts, offs, (int)nkeys, outE, outId);
-        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = launch_bucket_sort(starts, offs, (int)nkeys, outE, outId,
+                                    (int)std::min<long>(nkeys, (long)sm * 16), st)) != cudaSuccess)
+            break;
         e = cudaStreamSynchronize(st);
     } while (0);
     cudaFree(tmp);

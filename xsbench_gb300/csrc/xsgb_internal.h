@@ -178,6 +178,10 @@ xs_status launch_history(xs_ctx *ctx, cudaStream_t st, int arith, long first, lo
 xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long first, long count,
                                  int tile, int *launches);
 size_t batched_scratch_bytes(long count, int buckets);
+// Sorts each bucket [starts[b], ends[b]) of (sE, sid) by (energy order key,
+// id) in place (adjoint order, device setup); one block per bucket.
+cudaError_t launch_bucket_sort(const int *starts, const int *ends, int nbuckets, double *sE,
+                               int *sid, int blocks, cudaStream_t st);
 // Explicit device buffers of one batched run (every pointer into caller memory).
 struct BatchedScratch {
     unsigned long long *verification;
