@@ -14,8 +14,9 @@
 // bit-reproducible):
 //   1. counting sort by (material, energy bucket), then each bucket sorted by
 //      (energy, index) -- a deterministic total order per material;
-//   2. the upstream gradients gathered into that order;
-//   3. per lookup: forward macro_xs and dL/dE (interval search recomputed);
+//   2-3. per lookup: forward macro_xs and dL/dE (interval search
+//      recomputed), the upstream gradients gathered into sorted order on
+//      the way;
 //   4. chunk-local prefixes of g and g (E - Eref) over each chunk of 2,048
 //      sorted lookups; transposed pass: lanes take a chunk's nuclides, and each
 //      lane walks its nuclide's intervals across the chunk, finding the end of
@@ -248,21 +249,6 @@ cudaError_t launch_bucket_sort(const int *starts, const int *ends, int nbuckets,
     if (e != cudaSuccess) return e;
     k_bucket_sort<<<blocks, 256, sm, st>>>(starts, ends, nbuckets, sE, sid);
     return cudaGetLastError();
-}
-
-// gradients into sorted order (zeros on padding positions)
-__global__ void k_gather_gbar(const int *seg, const int *cnt, const int *sid, const double *gbar,
-                              double *sg)
-{
-    const int total = seg[kMaterials];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
-        int m = 0;
-        while (seg[m + 1] <= p) m++;
-        const bool valid = p < seg[m] + cnt[m];
-        const long id = valid ? sid[p] : 0;
-#pragma unroll
-        for (int c = 0; c < 5; c++) sg[(long)p * 5 + c] = valid ? gbar[id * 5 + c] : 0.0;
-    }
 }
 
 // ---------------------------------------------------- transposed layout ---
@@ -701,8 +687,6 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     if (s != XS_OK) return s;
     const int nbuckets = kMaterials * nb;
     XS_CUDA(launch_bucket_sort(starts, offs, nbuckets, sE, sid, std::min(nbuckets, ctx->sm_count * 8), st));
-    k_gather_gbar<<<ctx->sm_count * 8, 256, 0, st>>>(seg, cnt, sid, gbar, sg);
-    XS_CUDA(cudaGetLastError());
 
     // forward and dL/dE per lookup
     XS_CUDA(cudaMemsetAsync(queue, 0, 64, st));
@@ -720,10 +704,10 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     l.fuel_lanes = 1;
     l.table = 1;   // the forward reads the union table when there is one
     l.sorted = 1;
-    s = launch_adjoint_energy(ctx, st, l, sg, d_energy);
+    s = launch_adjoint_energy(ctx, st, l, gbar, sg, d_energy);
     if (s != XS_OK) return s;
 
-    int n = 7;
+    int n = 6;
     if (d_xs || d_concs) {
         XS_CUDA(cudaMemsetAsync(table, 0, (size_t)pairs * n_int * kTbl * 8, st));
         XS_CUDA(cudaMemsetAsync(queue + 4, 0, 4, st));

@@ -394,14 +394,14 @@ xs_status enqueue_sort_only(xs_ctx *ctx, cudaStream_t st, long first, long count
     return XS_OK;
 }
 
-xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l, const double *sg,
-                                double *d_energy)
+xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l,
+                                const double *gbar, double *sg, double *d_energy)
 {
     typedef cudaError_t (*AdjFn)(const Tables &, cudaStream_t, int, const ListArgs &,
-                                 const double *, double *);
+                                 const double *, double *, double *);
     const int g = ctx->t.grid_type;
     AdjFn f = g == XS_UNIONIZED ? unionized_adjoint : g == XS_NUCLIDE ? nuclide_adjoint : hash_adjoint;
-    XS_CUDA(f(ctx->t, st, ctx->sm_count * ctx->batched_blocks_per_sm, l, sg, d_energy));
+    XS_CUDA(f(ctx->t, st, ctx->sm_count * ctx->batched_blocks_per_sm, l, gbar, sg, d_energy));
     return XS_OK;
 }
 

@@ -420,11 +420,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_list_lookup_table(Tables t, ListA
 
 // ------------------------------------------------------- adjoint, energy ---
 // Over the adjoint's sorted list: the forward macro_xs (FAST arithmetic) and
-// dL/dE = sum_c gbar_c * sum_j conc_j * slope_jc, per lookup.  sg holds the
-// upstream gradients in sorted order (5 per position).
+// dL/dE = sum_c gbar_c * sum_j conc_j * slope_jc, per lookup.  gbar holds the
+// upstream gradients by lookup index; each lookup's five are also written to
+// sg in sorted order (5 per position, zeros on padding positions) for the
+// interval sums, so no separate gather pass runs.
 template <int GRID, bool TABLE = false>
-__global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, const double *sg,
-                                                         double *d_energy)
+__global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, const double *gbar,
+                                                         double *sg, double *d_energy)
 {
     __shared__ int seg[kMaterials + 1], cnt[kMaterials];
     __shared__ unsigned long long s_acc;
@@ -454,13 +456,21 @@ __global__ void __launch_bounds__(kBlock) k_list_adjoint(Tables t, ListArgs a, c
 #pragma unroll
                 for (int k = 0; k < 5; k++) a.out_macro[id * 5 + k] = macro[k];
             }
+            double g[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                g[k] = ldg(&gbar[id * 5 + k]);
+                sg[(long)p * 5 + k] = g[k];
+            }
             if (d_energy) {
-                const double *g = sg + (long)p * 5;
                 double dE = 0.0;
 #pragma unroll
                 for (int k = 0; k < 5; k++) dE = fma(g[k], S[k], dE);
                 d_energy[id] = dE;
             }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 5; k++) sg[(long)p * 5 + k] = 0.0;
         }
     }
     block_verification(mine, &s_acc, a.verif);
@@ -592,7 +602,7 @@ struct GridLaunch {
     cudaError_t NAME##_history(const Tables &t, cudaStream_t st, int arith, long first,         \
                                long count, int nl, unsigned long long *verif, int *err);        \
     cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
-                               const double *sg, double *d_energy);
+                               const double *gbar, double *sg, double *d_energy);
 XSGB_DECLARE_GRID(unionized)
 XSGB_DECLARE_GRID(nuclide)
 XSGB_DECLARE_GRID(hash)
@@ -614,15 +624,15 @@ XSGB_DECLARE_GRID(hash)
         return GridLaunch<GRID>::history(t, st, arith, first, count, nl, verif, err);           \
     }                                                                                           \
     cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
-                               const double *sg, double *d_energy)                              \
+                               const double *gbar, double *sg, double *d_energy)                \
     {                                                                                           \
         if constexpr (GRID == XS_UNIONIZED) {                                                   \
             if (a.table && t.utab[0] != nullptr) {                                              \
-                k_list_adjoint<GRID, true><<<blocks, kBlock, 0, st>>>(t, a, sg, d_energy);      \
+                k_list_adjoint<GRID, true><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy); \
                 return cudaGetLastError();                                                      \
             }                                                                                   \
         }                                                                                       \
-        k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, sg, d_energy);                    \
+        k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy);              \
         return cudaGetLastError();                                                              \
     }
 

@@ -207,8 +207,8 @@ struct ListArgs;
 xs_status enqueue_sort_only(xs_ctx *ctx, cudaStream_t st, long first, long count, int nb_log2,
                             const SampleInput &in, int *offs, int *starts, int *seg, int *cnt,
                             double *sE, int *sid);
-xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l, const double *sg,
-                                double *d_energy);
+xs_status launch_adjoint_energy(xs_ctx *ctx, cudaStream_t st, const ListArgs &l,
+                                const double *gbar, double *sg, double *d_energy);
 // adjoint.cu: the whole adjoint on `st` (all pointers device memory)
 xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
                          const SampleInput &in, const double *gbar, double *macro_out,
