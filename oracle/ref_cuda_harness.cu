@@ -9,10 +9,14 @@
 // cubin with the driver API and launches the reference's kernels:
 //   -k 0  xs_lookup_kernel_baseline, 256 threads per block
 //         (cuda/Simulation.cu:15-38)
-//   -k 6  sampling_kernel, then the samples sorted by material and energy on
-//         the host (the thrust sorts of cuda/Simulation.cu:1062-1076, not
-//         timed), then xs_lookup_kernel_optimization_4 once per material with
-//         32 threads per block (:1078-1086)
+//   -k 1..6  sampling_kernel, then the optimisations' lookup launches, 32
+//         threads per block: 1 one kernel (:464), 2 one per material over all
+//         samples (:576), 3 fuel and non-fuel over all samples (:692), 4 the
+//         samples sorted by material, one launch per material (:823), 5 fuel
+//         partitioned first, two launches (:960), 6 sorted by material and
+//         energy, one launch per material of the optimisation-4 kernel
+//         (:1062-1086); the thrust sorts / partition run on the host here and
+//         are not timed
 // Only the lookup launches are timed (CUDA events); the per-lookup
 // verification array is summed on the host afterwards.  Output: one JSON line.
 #include <cuda.h>
@@ -148,45 +152,92 @@ int main(int argc, char **argv)
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (r) times.push_back(ms);
         }
-    } else if (kernel == 6) {
-        what = "sampling_kernel, host sort by (material, energy), 12 x xs_lookup_kernel_optimization_4 "
-               "(cuda/Simulation.cu:823), 32 threads/block; lookups timed";
+    } else if (kernel >= 1 && kernel <= 6) {
+        // cuda/Simulation.cu:388-1099: sampling_kernel, then per variant
+        // (samples reordered on the host where the reference runs thrust;
+        // not timed) the lookup launches, 32 threads per block
+        static const char *whats[7] = {
+            "",
+            "sampling_kernel, xs_lookup_kernel_optimization_1 (cuda/Simulation.cu:464); lookups timed",
+            "sampling_kernel, 12 x xs_lookup_kernel_optimization_2 (cuda/Simulation.cu:576), one per "
+            "material over all samples; lookups timed",
+            "sampling_kernel, 2 x xs_lookup_kernel_optimization_3 (cuda/Simulation.cu:692), fuel and "
+            "non-fuel over all samples; lookups timed",
+            "sampling_kernel, host sort by material, 12 x xs_lookup_kernel_optimization_4 "
+            "(cuda/Simulation.cu:823); lookups timed",
+            "sampling_kernel, host partition fuel first, 2 x xs_lookup_kernel_optimization_5 "
+            "(cuda/Simulation.cu:960); lookups timed",
+            "sampling_kernel, host sort by (material, energy), 12 x xs_lookup_kernel_optimization_4 "
+            "(cuda/Simulation.cu:823), 32 threads/block; lookups timed"};
+        what = whats[kernel];
         CK(cudaMalloc((void **)&g.p_energy_samples, N * sizeof(double)));
         CK(cudaMalloc((void **)&g.mat_samples, N * sizeof(int)));
         g.length_p_energy_samples = g.length_mat_samples = (int)N;
-        CUfunction fs, f4;
+        CUfunction fs, fk;
         CKD(cuModuleGetFunction(&fs, mod, "_Z15sampling_kernel6Inputs14SimulationData"));
-        CKD(cuModuleGetFunction(&f4, mod, "_Z31xs_lookup_kernel_optimization_46Inputs14SimulationDataiii"));
+        static const char *names[7] = {
+            "", "_Z31xs_lookup_kernel_optimization_16Inputs14SimulationData",
+            "_Z31xs_lookup_kernel_optimization_26Inputs14SimulationDatai",
+            "_Z31xs_lookup_kernel_optimization_36Inputs14SimulationDatai",
+            "_Z31xs_lookup_kernel_optimization_46Inputs14SimulationDataiii",
+            "_Z31xs_lookup_kernel_optimization_56Inputs14SimulationDataii",
+            "_Z31xs_lookup_kernel_optimization_46Inputs14SimulationDataiii"};
+        CKD(cuModuleGetFunction(&fk, mod, names[kernel]));
         void *sp[] = {&in, &g};
-        CKD(cuLaunchKernel(fs, (unsigned)((N + 31) / 32), 1, 1, 32, 1, 1, 0, 0, sp, nullptr));
+        const unsigned all_blocks = (unsigned)((N + 31) / 32);
+        CKD(cuLaunchKernel(fs, all_blocks, 1, 1, 32, 1, 1, 0, 0, sp, nullptr));
         CK(cudaDeviceSynchronize());
-        std::vector<double> E(N);
-        std::vector<int> M(N);
-        CK(cudaMemcpy(E.data(), g.p_energy_samples, N * 8, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(M.data(), g.mat_samples, N * 4, cudaMemcpyDeviceToHost));
-        std::vector<long> order(N);
-        std::iota(order.begin(), order.end(), 0L);
-        std::sort(order.begin(), order.end(), [&](long a, long b) {
-            return M[a] != M[b] ? M[a] < M[b] : E[a] < E[b];
-        });
-        std::vector<double> E2(N);
-        std::vector<int> M2(N);
-        for (long i = 0; i < N; i++) {
-            E2[i] = E[order[i]];
-            M2[i] = M[order[i]];
-            counts[M2[i]]++;
+        int n_fuel = 0;
+        if (kernel >= 4) {
+            std::vector<double> E(N);
+            std::vector<int> M(N);
+            CK(cudaMemcpy(E.data(), g.p_energy_samples, N * 8, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(M.data(), g.mat_samples, N * 4, cudaMemcpyDeviceToHost));
+            std::vector<long> order(N);
+            std::iota(order.begin(), order.end(), 0L);
+            if (kernel == 4)       // thrust::sort_by_key on the materials (:797)
+                std::stable_sort(order.begin(), order.end(), [&](long a, long b) { return M[a] < M[b]; });
+            else if (kernel == 5)  // thrust::partition, fuel first (:936)
+                std::stable_partition(order.begin(), order.end(), [&](long a) { return M[a] == 0; });
+            else                   // by material, then energy within each (:1067-1076)
+                std::sort(order.begin(), order.end(), [&](long a, long b) {
+                    return M[a] != M[b] ? M[a] < M[b] : E[a] < E[b];
+                });
+            std::vector<double> E2(N);
+            std::vector<int> M2(N);
+            for (long i = 0; i < N; i++) {
+                E2[i] = E[order[i]];
+                M2[i] = M[order[i]];
+                counts[M2[i]]++;
+            }
+            n_fuel = counts[0];
+            CK(cudaMemcpy(g.p_energy_samples, E2.data(), N * 8, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(g.mat_samples, M2.data(), N * 4, cudaMemcpyHostToDevice));
         }
-        CK(cudaMemcpy(g.p_energy_samples, E2.data(), N * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(g.mat_samples, M2.data(), N * 4, cudaMemcpyHostToDevice));
         for (int r = 0; r < reps + 1; r++) {
             CK(cudaEventRecord(e0));
-            int offset = 0;
-            for (int m = 0; m < 12; m++) {
-                int n_m = counts[m];
-                void *p4[] = {&in, &g, &m, &n_m, &offset};
-                const unsigned blocks = (unsigned)((n_m + 31) / 32);
-                if (blocks) CKD(cuLaunchKernel(f4, blocks, 1, 1, 32, 1, 1, 0, 0, p4, nullptr));
-                offset += n_m;
+            if (kernel == 1) {
+                CKD(cuLaunchKernel(fk, all_blocks, 1, 1, 32, 1, 1, 0, 0, sp, nullptr));
+            } else if (kernel == 2 || kernel == 3) {
+                for (int m = 0; m < (kernel == 2 ? 12 : 2); m++) {
+                    void *p2[] = {&in, &g, &m};
+                    CKD(cuLaunchKernel(fk, all_blocks, 1, 1, 32, 1, 1, 0, 0, p2, nullptr));
+                }
+            } else if (kernel == 5) {
+                int n0 = n_fuel, o0 = 0, n1 = (int)N - n_fuel, o1 = n_fuel;
+                void *p5a[] = {&in, &g, &n0, &o0};
+                void *p5b[] = {&in, &g, &n1, &o1};
+                if (n0) CKD(cuLaunchKernel(fk, (unsigned)((n0 + 31) / 32), 1, 1, 32, 1, 1, 0, 0, p5a, nullptr));
+                if (n1) CKD(cuLaunchKernel(fk, (unsigned)((n1 + 31) / 32), 1, 1, 32, 1, 1, 0, 0, p5b, nullptr));
+            } else {
+                int offset = 0;
+                for (int m = 0; m < 12; m++) {
+                    int n_m = counts[m];
+                    void *p4[] = {&in, &g, &m, &n_m, &offset};
+                    const unsigned blocks = (unsigned)((n_m + 31) / 32);
+                    if (blocks) CKD(cuLaunchKernel(fk, blocks, 1, 1, 32, 1, 1, 0, 0, p4, nullptr));
+                    offset += n_m;
+                }
             }
             CK(cudaEventRecord(e1));
             CK(cudaEventSynchronize(e1));
@@ -195,7 +246,7 @@ int main(int argc, char **argv)
             if (r) times.push_back(ms);
         }
     } else {
-        fprintf(stderr, "kernel %d: use 0 or 6\n", kernel);
+        fprintf(stderr, "kernel %d: use 0 to 6\n", kernel);
         return 1;
     }
     std::vector<unsigned long> v(N);
