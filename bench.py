@@ -302,9 +302,15 @@ def main():
     # the published hash holds for the workload as defined (not for a resized one)
     expected = None if args.gridpoints else X.EXPECTED_HASH.get(("event", wl["size"].lower()))
     hash_ok = (expected is None or rank != 0 or N != 17000000 or r.hash == expected)
-    for _ in range(args.warmup):
+    # W warm-up steps, continued until the GPU has been busy for about a
+    # second: a freshly started GPU ran the first ~20 steps measurably slower
+    # (3 warm-up steps: 849-863 M lookups/s in the first process on a box,
+    # 893 M in the next; 60 warm-up steps: 893 M in the first)
+    warm, t_warm = 0, time.perf_counter()
+    while warm < args.warmup or (time.perf_counter() - t_warm < 1.0 and warm < 200):
         ctx.run_event(async_=True, **kw)
-    ctx.sync()
+        ctx.sync()
+        warm += 1
 
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -408,7 +414,7 @@ def main():
             cpu = cpu_baseline_oracle(inputs, problem, args.workload, args.cpu_budget)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
+            "steps": args.steps, "warmup": warm,
             "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the reference's own LCG problem generators)",
