@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "lcg_bits.h"
 #include "xsgb_internal.h"
 
 namespace xsgb {
@@ -19,11 +20,16 @@ namespace xsgb {
 constexpr unsigned long long kLcgMul = 2806196910506780709ULL;
 constexpr unsigned long long kLcgMask = (1ULL << 63) - 1ULL;
 
+__host__ __device__ __forceinline__ unsigned long long lcg_step(unsigned long long s)
+{
+    return (kLcgMul * s + 1ULL) & kLcgMask;
+}
+
 __host__ __device__ __forceinline__ double lcg_next(unsigned long long &s)
 {
-    s = (kLcgMul * s + 1ULL) & kLcgMask;
+    s = lcg_step(s);
 #ifdef __CUDA_ARCH__
-    return __dmul_rn(__ull2double_rn(s), 0x1p-63);  // exact scaling by 2^-63
+    return xsgb_lcg_value(s);   // the same bits, on the integer pipe
 #else
     return (double)s * 0x1p-63;
 #endif
@@ -47,13 +53,15 @@ __host__ __device__ __forceinline__ unsigned long long lcg_skip(unsigned long lo
 }
 
 // Simulation.c:426-460: the first material whose running sum exceeds the roll;
-// the running sums are precomputed on the host in the reference's order.
+// the running sums are precomputed on the host in the reference's order, and
+// `roll < sum` is compared as `state < mat_tseed` (the smallest state whose
+// draw reaches the sum), which gives the same material without forming the roll.
 __device__ __forceinline__ int pick_mat(const Tables &t, unsigned long long &s)
 {
-    double roll = lcg_next(s);
+    s = lcg_step(s);
 #pragma unroll
     for (int m = 1; m < kMaterials; m++)
-        if (roll < t.mat_thresh[m]) return m;
+        if (s < t.mat_tseed[m]) return m;
     return 0;
 }
 
@@ -457,7 +465,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
         const double dl = E - ldg(&t.union_e[row]);
         const double2 *blk = t.utab[mat] + row * n * 5;
         const unsigned long long pol = policy_first();
-        if (DE) {
+        if constexpr (DE) {
             // with the energy derivative: macro = sum conc * v + dl * S, where
             // S = sum conc * s is the derivative itself, so 10 FP64 operations
             // per nuclide instead of 15 (every |s * dl| is at most the
@@ -481,8 +489,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             }
 #pragma unroll
             for (int k = 0; k < 5; k++) macro[k] = fma(dl, S[k], macro[k]);
-            return;
-        }
+        } else {
 #pragma unroll 4
         for (int j = q0; j < n; j += stride) {
             const double2 *p = blk + (long)j * 5;
@@ -494,6 +501,7 @@ __device__ __forceinline__ void macro_xs_unionized(const Tables &t, double E, in
             macro[2] = fma(fma(a2.y, dl, a2.x), conc, macro[2]);
             macro[3] = fma(fma(a3.y, dl, a3.x), conc, macro[3]);
             macro[4] = fma(fma(a4.y, dl, a4.x), conc, macro[4]);
+        }
         }
         return;
     }

@@ -56,13 +56,15 @@ __global__ void __launch_bounds__(kBlock) k_sort_pass(Tables t, long first, long
         if (i0 >= count) return;
         unsigned long long seed = lcg_skip(kStartingSeed, 2ULL * (unsigned long long)(first + i0));
         for (int q = 0; q < kSortLpt && i0 + q < count; q++) {
-            double E;
-            int m;
-            sample_at<false>(t, nullptr, nullptr, 0, seed, E, m, err);
-            const int key = (m << nb_log2) + energy_bucket(E, nb_log2);
+            // the energy draw's state; its bucket floor(E * nb) and (when
+            // scattering) E itself come from it on the integer pipe
+            seed = lcg_step(seed);
+            const unsigned long long es = seed;
+            const int m = pick_mat(t, seed);
+            const int key = (m << nb_log2) + xsgb_lcg_bucket(es, nb_log2);
             if (SCATTER) {
                 const int pos = atomicAdd(&offs[key], 1);
-                sE[pos] = E;
+                sE[pos] = xsgb_lcg_value(es);
                 sid[pos] = (int)(i0 + q);
             } else {
                 atomicAdd(&offs[key], 1);

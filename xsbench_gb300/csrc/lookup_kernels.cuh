@@ -581,6 +581,19 @@ struct GridLaunch {
 #undef XSGB_LIST
     }
 
+    static cudaError_t adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a,
+                               const double *gbar, double *sg, double *d_energy)
+    {
+        if constexpr (GRID == XS_UNIONIZED) {
+            if (a.table && t.utab[0] != nullptr) {
+                k_list_adjoint<GRID, true><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy);
+                return cudaGetLastError();
+            }
+        }
+        k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy);
+        return cudaGetLastError();
+    }
+
     static cudaError_t history(const Tables &t, cudaStream_t st, int arith, long first,
                                long count, int nl, unsigned long long *verif, int *err)
     {
@@ -626,14 +639,7 @@ XSGB_DECLARE_GRID(hash)
     cudaError_t NAME##_adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a, \
                                const double *gbar, double *sg, double *d_energy)                \
     {                                                                                           \
-        if constexpr (GRID == XS_UNIONIZED) {                                                   \
-            if (a.table && t.utab[0] != nullptr) {                                              \
-                k_list_adjoint<GRID, true><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy); \
-                return cudaGetLastError();                                                      \
-            }                                                                                   \
-        }                                                                                       \
-        k_list_adjoint<GRID><<<blocks, kBlock, 0, st>>>(t, a, gbar, sg, d_energy);              \
-        return cudaGetLastError();                                                              \
+        return GridLaunch<GRID>::adjoint(t, st, blocks, a, gbar, sg, d_energy);                 \
     }
 
 }  // namespace xsgb

@@ -48,6 +48,7 @@ struct Tables {
     const int *union_bins;           // [2^b + 1]
     const int *index_grid;           // UEG: [n_union * n_iso]  HASH: [hash_bins * n_iso]
     double mat_thresh[kMaterials];   // pick_mat running sums, Simulation.c:450-457
+    unsigned long long mat_tseed[kMaterials];  // smallest LCG state whose draw reaches each sum
     int mat_lo[kMaterials];          // smallest / largest nuclide id of each material
     int mat_hi[kMaterials];          //   (span of the index-row prefetch)
     unsigned hot[16];                // nuclides (< 512) whose records stay in L2 (evict_last)
