@@ -307,6 +307,7 @@ xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
     t.grid_type = in->grid_type;
     t.hash_bins = in->hash_bins;
     t.hash_du = in->hash_bins > 0 ? 1.0 / in->hash_bins : 0.0;
+    t.hash_margin = xsgb_hash_margin_bits(in->hash_bins);
     pick_mat_thresholds(t.mat_thresh);
     for (int m = 0; m < kMaterials; m++) t.mat_tseed[m] = xsgb_lcg_threshold(t.mat_thresh[m]);
     *out = ctx;

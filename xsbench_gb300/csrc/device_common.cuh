@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bin_bits.h"
 #include "lcg_bits.h"
 #include "xsgb_internal.h"
 
@@ -118,10 +119,10 @@ __device__ __forceinline__ long union_row(const Tables &t, double E)
 {
     const long n = t.n_union;
     long c;
-    if (E >= 0.0 && E < 1.0) {
-        const int b = (int)(E * (double)(1 << t.union_bin_log2));
+    const long long q = order_key(E);
+    if (q >= 0 && q < 0x3FF0000000000000LL) {   // E in [0, 1) (-0 included, NaN not)
+        const int b = xsgb_floor_scaled_pow2(E, t.union_bin_log2);   // floor(E * 2^k)
         long lo = ldg(&t.union_bins[b]), hi = ldg(&t.union_bins[b + 1]);
-        const long long q = order_key(E);
         while (lo < hi) {
             long mid = (lo + hi) >> 1;
             if (ldg(&t.union_keys[mid]) <= q) lo = mid + 1; else hi = mid;
@@ -585,11 +586,15 @@ __device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E,
     long bin = 0, bin_min = -1;
     bool outside = false;   // E not in [bin*du, (bin+1)*du)
     if (HASHQ) {
-        bin = (long)(E / t.hash_du);   // Simulation.c:350-351
-        if (bin < 0) bin = 0;
-        if (bin > t.hash_bins - 1) bin = t.hash_bins - 1;
-        outside = (double)bin * t.hash_du > E ||
-                  (bin < t.hash_bins - 1 && (double)(bin + 1) * t.hash_du <= E);
+        // Simulation.c:350-351; away from bin edges the bin is exact in
+        // integers, and E then lies inside it
+        if (!xsgb_hash_bin(E, (uint32_t)t.hash_bins, t.hash_margin, &bin)) {
+            bin = (long)(E / t.hash_du);
+            if (bin < 0) bin = 0;
+            if (bin > t.hash_bins - 1) bin = t.hash_bins - 1;
+            outside = (double)bin * t.hash_du > E ||
+                      (bin < t.hash_bins - 1 && (double)(bin + 1) * t.hash_du <= E);
+        }
         // the bin of the warp's lowest live energy, when that energy lies in it
         const bool is_min = live && q == qmin;
         const unsigned owners = __ballot_sync(0xffffffffu, is_min);
@@ -662,11 +667,14 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
     if (GRID == XS_UNIONIZED) {
         row = union_row(t, E);
     } else if (GRID == XS_HASH) {
-        row = (long)(E / t.hash_du);  // Simulation.c:350-351
-        if (row < 0 || row > t.hash_bins - 1) {
-            // the reference reads outside its table here; clamp instead
-            if (CHECKED) report(err, XS_ERR_DATA, row, -1);
-            row = row < 0 ? 0 : t.hash_bins - 1;
+        // Simulation.c:350-351 (away from bin edges exact in integers)
+        if (!xsgb_hash_bin(E, (uint32_t)t.hash_bins, t.hash_margin, &row)) {
+            row = (long)(E / t.hash_du);
+            if (row < 0 || row > t.hash_bins - 1) {
+                // the reference reads outside its table here; clamp instead
+                if (CHECKED) report(err, XS_ERR_DATA, row, -1);
+                row = row < 0 ? 0 : t.hash_bins - 1;
+            }
         }
         q = order_key(E);
     } else {

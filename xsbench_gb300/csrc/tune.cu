@@ -65,6 +65,7 @@ static void apply_view(Tables &t, const GridView &v)
     t.grid_type = v.grid_type;
     t.hash_bins = v.hash_bins;
     t.hash_du = v.hash_du;
+    t.hash_margin = xsgb_hash_margin_bits(v.hash_bins);
     t.index_grid = v.index_grid;
     t.coarse = v.coarse;
     t.n_coarse = v.n_coarse;

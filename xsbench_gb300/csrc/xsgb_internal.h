@@ -33,6 +33,7 @@ struct Tables {
     int hash_bins;
     int max_nucs;
     double hash_du;                  // 1.0 / hash_bins, as the reference computes it
+    int hash_margin;                 // xsgb_hash_margin_bits(hash_bins)
     long n_union;
     int union_bin_log2;              // union accelerator: 2^b bins over [0,1)
     int n_coarse;                    // coarse keys per nuclide (NUCLIDE grid)
