@@ -550,9 +550,15 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
                                  int tile, int *launches)
 {
     const int nl = ctx->inputs.lookups;
-    if (tile <= 0) tile = 256;   // a step is one batch of `count` lookups: small tiles fill the GPU
-    const size_t ps_bytes = plain_scratch_bytes(count, tile);
-    const size_t need = (size_t)count * (8 + 8 + 4 + 40) + ps_bytes + 4096;
+    // A step is one batch of `count` lookups (500,000 at the default size),
+    // too few to fill the GPU, so each step lasts about as long as its
+    // longest fuel lookups: FAST (fuel over 4 lanes) wants small tiles,
+    // EXACT (fuel on one lane, 321 nuclides in order) large ones; and the
+    // overflow pass would add one more such chain per step (measured, large
+    // problem: FAST 609 M lookups/s at 256 with no overflow pass, EXACT 172 M
+    // at 2,048 against 115-130 M with the pass)
+    if (tile <= 0) tile = arith == XS_ARITH_EXACT ? 2048 : 256;
+    const size_t need = (size_t)count * (8 + 8 + 4 + 40) + 4096;
     if (ctx->s.hist_bytes < need) {
         if (ctx->s.hist_buf) {
             cudaFree(ctx->s.hist_buf);
@@ -574,8 +580,6 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
     double *E = (double *)take((size_t)count * 8);
     int *mat = (int *)take((size_t)count * 4);
     double *macro = (double *)take((size_t)count * 40);
-    PlainScratch ps = carve_plain_scratch(take(ps_bytes), count, tile);
-    const bool ovf = count > 8L * tile && ctx->t.grid_type != XS_NUCLIDE;
     const unsigned blocks = (unsigned)std::min<long>((count + 255) / 256, (long)ctx->sm_count * 16);
     k_history_init<<<blocks, 256, 0, st>>>(ctx->t, first, count, nl, seed, E, mat);
     XS_CUDA(cudaGetLastError());
@@ -586,7 +590,7 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
     Outputs out;
     out.macro = macro;
     for (int step = 0; step < nl; step++) {
-        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, in, out, ovf ? &ps : nullptr, &n);
+        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, in, out, nullptr, &n);
         if (s != XS_OK) return s;
         if (step + 1 < nl) {
             k_history_advance<<<blocks, 256, 0, st>>>(ctx->t, count, macro, seed, E, mat);

@@ -523,7 +523,10 @@ struct GridLaunch {
                              bool samples, const PlainArgs &a)
     {
         const long blocks = (a.count + a.tile - 1) / a.tile;
-        const bool srow = a.stage_rows && a.rows_total > 0 &&
+        // staged rows: FAST, unchecked (the variants instantiated with them);
+        // the others keep the smaller shared-memory carveout (and their L1)
+        const bool srow = a.stage_rows && a.rows_total > 0 && !checked &&
+                          arith != XS_ARITH_EXACT &&
                           plain_smem_bytes(a.tile, a.rows_total) <= 96 * 1024;
         const size_t sm = plain_smem_bytes(a.tile, srow ? a.rows_total : 0);
         // shared-memory share of the SM's 228 KB that holds the resident
@@ -543,7 +546,7 @@ struct GridLaunch {
         return cudaGetLastError();                                                            \
     } while (0)
 #define XSGB_PLAIN(A, C, S) XSGB_PLAIN_R(A, C, S, false)
-        if (srow && !checked && arith != XS_ARITH_EXACT) {
+        if (srow) {
             if (samples) XSGB_PLAIN_R(XS_ARITH_FAST, false, true, true);
             XSGB_PLAIN_R(XS_ARITH_FAST, false, false, true);
         }
