@@ -20,11 +20,13 @@ namespace xsgb {
 // ------------------------------------------------------------ sort pass ---
 constexpr int kSortLpt = 8;  // lookups per thread in the sampling passes
 
+// floor(E * 2^nb_log2) for E in [0, 1), on the integer pipe
 __device__ __forceinline__ int energy_bucket(double E, int nb_log2)
 {
-    const int nb = 1 << nb_log2;
-    if (E >= 0.0 && E < 1.0) return (int)(E * (double)nb);
-    return (E >= 1.0) ? nb - 1 : 0;  // NaN and negatives go to bucket 0
+    const long long q = order_key(E);
+    if (q >= 0 && q < 0x3FF0000000000000LL) return xsgb_floor_scaled_pow2(E, nb_log2);
+    return (q >= 0x3FF0000000000000LL && q <= 0x7FF0000000000000LL) ? (1 << nb_log2) - 1
+                                                                   : 0;  // NaN and negatives: 0
 }
 
 template <bool SAMPLES, bool SCATTER>
