@@ -8,7 +8,7 @@ import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
-from xsbench_gb300.shard import reduce_time_max, reduce_verification, shard_range
+from xsbench_gb300.shard import reduce_gradients, reduce_time_max, reduce_verification, shard_range
 
 
 def _free_port():
@@ -67,3 +67,60 @@ def test_shard_range_partitions():
         assert [shard_range(r, world, n, "weak") for r in range(world)] == [(r * n, n) for r in range(world)]
     with pytest.raises(ValueError):
         shard_range(2, 2, 10)
+
+
+def _grad_worker(rank, world, port, n, out):
+    """Rank's shard of an adjoint batch: gradients of its lookups with the
+    plain-PyTorch reference (the adjoint's own checker; no GPU here), then the
+    rank-order reduction."""
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import numpy as np
+    import torch
+    import oracle
+    from conftest import oracle_config
+    from torch_reference import reference_gradients, tables_from_arrays
+    first, count = shard_range(rank, world, n, "strong")
+    with oracle.Problem(oracle_config("tiny_unionized")) as p:
+        arrs = p.arrays()
+        r = p.run_event(first=first, n=count, want_samples=True, nthreads=1)
+        egrid, xs, concs, mats, nn = tables_from_arrays(arrs, 68, 1000, 34)
+    g = np.random.default_rng(77).standard_normal((n, 5))[first:first + count]
+    _, _, dc, dx = reference_gradients(r["energy"], r["mat"], g, egrid, xs, concs, mats, nn)
+    red = reduce_gradients([torch.from_numpy(dc), torch.from_numpy(dx)], dist)
+    out[rank] = (dc, dx, red[0].numpy(), red[1].numpy())
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_reduce_adjoint_gradients_in_rank_order():
+    """The ranks' dL/dconcs and dL/dxs, reduced, are the same bits on every
+    rank and equal the rank-order sum of the partial gradients; they match
+    the single-process gradient of the whole batch within rounding."""
+    import numpy as np
+    import oracle
+    from conftest import oracle_config
+    from torch_reference import reference_gradients, tables_from_arrays
+    n, world = 6000, 2
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_grad_worker, args=(r, world, port, n, out)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(300)
+        assert p.exitcode == 0
+    serial_c = out[0][0] + out[1][0]
+    serial_x = out[0][1] + out[1][1]
+    for r in range(world):
+        assert np.array_equal(out[r][2], serial_c)
+        assert np.array_equal(out[r][3], serial_x)
+    with oracle.Problem(oracle_config("tiny_unionized")) as p:
+        arrs = p.arrays()
+        s = p.run_event(first=0, n=n, want_samples=True, nthreads=1)
+        egrid, xs, concs, mats, nn = tables_from_arrays(arrs, 68, 1000, 34)
+    g = np.random.default_rng(77).standard_normal((n, 5))
+    _, _, dc, dx = reference_gradients(s["energy"], s["mat"], g, egrid, xs, concs, mats, nn)
+    assert np.max(np.abs(serial_c - dc)) <= 1e-12 * np.max(np.abs(dc))
+    assert np.max(np.abs(serial_x - dx)) <= 1e-12 * np.max(np.abs(dx))

@@ -1,7 +1,9 @@
 """Host logic of multi-GPU runs: one process per GPU, each on its own range
 of event indices (lookup i's sample is a pure function of i, so ranges need
-no exchange).  The only collectives are the sum of the verification partials
-(exact in any order: integers) and the max of the ranks' timed spans."""
+no exchange).  The collectives are the sum of the verification partials
+(exact in any order: integers), the max of the ranks' timed spans and, for
+the adjoint, the sum of the ranks' gradient arrays in rank order (floating
+point: a fixed order keeps the result bit-reproducible)."""
 from __future__ import annotations
 
 
@@ -41,3 +43,24 @@ def reduce_time_max(seconds: float, dist=None) -> float:
         t = t.cuda()
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def reduce_gradients(arrays, dist=None):
+    """Sum each rank's gradient arrays (dL/dconcs, dL/dxs: tensors of the same
+    shape on every rank) into every rank, adding the ranks' contributions in
+    rank order 0, 1, ..., so the bits do not depend on the collective's own
+    reduction order.  Returns new tensors; a single process gets copies."""
+    import torch
+    arrays = list(arrays)
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return [a.clone() for a in arrays]
+    world = dist.get_world_size()
+    out = []
+    for a in arrays:
+        parts = [torch.empty_like(a) for _ in range(world)]
+        dist.all_gather(parts, a.contiguous())
+        acc = parts[0].clone()
+        for p in parts[1:]:
+            acc += p
+        out.append(acc)
+    return out
