@@ -113,21 +113,22 @@ __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, 
     return (unsigned)(arg + 1);
 }
 
-// One fuel (material 0) lookup spread over L lanes, FAST arithmetic: lane q
-// sums the nuclides j = q, q + L, ...; the partial sums are added in the fixed
-// tree (q0 + q1) + (q2 + q3), which gives the same bits on every lane of the
-// lookup.  Every lane of the warp calls this (shuffles); `live` is the same on
-// the L lanes of a lookup.  Returns argmax+1 on the lookup's lane q == 0.
+// One lookup of material m (the fuel, or a tile's partial chunk) spread over
+// L lanes, FAST arithmetic: lane q sums the nuclides j = q, q + L, ...; the
+// partial sums are added in the fixed tree (q0 + q1) + (q2 + q3), which gives
+// the same bits on every lane of the lookup.  Every lane of the warp calls
+// this (shuffles); `live` is the same on the L lanes of a lookup.  Returns
+// argmax+1 on the lookup's lane q == 0.
 template <int GRID, bool CHECKED, bool TABLE, bool SROW = false>
 __device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool live, double E,
                                                            long o, int q, int L,
                                                            double *out_macro,
                                                            unsigned char *out_idx, int *err,
-                                                           SRows sr = SRows())
+                                                           SRows sr = SRows(), int m = 0)
 {
     double macro[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     if (live)
-        macro_xs<GRID, XS_ARITH_FAST, CHECKED, false, TABLE, SROW>(t, E, 0, macro, err, nullptr, q,
+        macro_xs<GRID, XS_ARITH_FAST, CHECKED, false, TABLE, SROW>(t, E, m, macro, err, nullptr, q,
                                                                    L, sr);
     for (int s = 1; s < L; s <<= 1) {
 #pragma unroll
@@ -333,6 +334,22 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
         int m = 0;
         while (seg[m + 1] <= cv * 32) m++;
         const int limit = seg[m] + (overflow ? (cnt[m] & ~31) : cnt[m]);
+        if constexpr (SAMPLES && ARITH == XS_ARITH_FAST) {
+            // Without the overflow pass (the chunked pipelines of caller
+            // samples), a material's last chunk is partial: its lookups take
+            // 2 or 4 lanes each, so the chunk's warp does not idle half its
+            // lanes through the nuclide loop.
+            const int live_n = limit - cv * 32;   // warp-uniform
+            if (!overflow && live_n < 16) {
+                const int Lp = live_n <= 8 ? 4 : 2;
+                const int q = lane & (Lp - 1), pl = lane / Lp;
+                const bool live = pl < live_n;
+                const int l = live ? perm[cv * 32 + pl] : 0;
+                mine += split_lookup_and_store<GRID, CHECKED, false, SROW>(
+                    t, live, sE[l], base + l, q, Lp, a.out_macro, a.out_idx, a.err, sr, m);
+                continue;
+            }
+        }
         if (p < limit) {
             const int l = perm[p];
             mine += lookup_and_store<GRID, ARITH, CHECKED, false, SROW>(
