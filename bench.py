@@ -43,6 +43,8 @@ WORKLOADS = {
     "large_hash": dict(size="large", grid="hash"),
     "large_nuclide": dict(size="large", grid="nuclide"),
     "small_unionized": dict(size="small", grid="unionized"),
+    "small_hash": dict(size="small", grid="hash"),
+    "small_nuclide": dict(size="small", grid="nuclide"),
     "xl_hash": dict(size="XL", grid="hash", lookups=100000000),
     "xl_nuclide": dict(size="XL", grid="nuclide", lookups=100000000),
 }
@@ -157,9 +159,31 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def cpu_k1(L, inp, sd, lookups, cores, budget_s):
+    """The port of the reference's optimisation 1 (Simulation.c:698-871:
+    sampling, sorts by material and energy, lookups by material) over the
+    first n lookups, n sized to about budget_s seconds; (rate, record)."""
+    ph = (C.c_double * 4)()
+    n = min(lookups, 1000000)
+    t0 = time.perf_counter()
+    L.or_run_event_k1(C.byref(inp), sd, 0, n, cores, ph)
+    dt = time.perf_counter() - t0
+    n2 = int(min(lookups, max(n, n * budget_s / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    L.or_run_event_k1(C.byref(inp), sd, 0, n2, cores, ph)
+    dt2 = time.perf_counter() - t0
+    return n2 / dt2, {"value": n2 / dt2, "unit": UNIT,
+                      "sample": f"lookups [0, {n2}) sampled, sorted and looked up in one call, "
+                                f"{dt2:.2f} s on {cores} threads",
+                      "phases_s": {"sample": round(ph[0], 3), "sort": round(ph[1], 3),
+                                   "lookup": round(ph[2], 3)}}
+
+
 def cpu_baseline_oracle(inputs_x, problem, workload, budget_s=10.0):
-    """The oracle port timed on this host's cores over a bounded sample of the
-    same workload, reusing the (bit-identical) setup arrays."""
+    """The oracle port of the reference's CPU path timed on this host's cores
+    over bounded samples of the same workload, reusing the (bit-identical)
+    setup arrays: the event loop (k0, Simulation.c:15-114; the line's value)
+    and optimisation 1 (k1, Simulation.c:698-871)."""
     import oracle
     L = oracle.lib()
     oin = oracle.Inputs()
@@ -174,9 +198,12 @@ def cpu_baseline_oracle(inputs_x, problem, workload, budget_s=10.0):
     t0 = time.perf_counter()
     L.or_run_event(C.byref(oin), sd, 0, n2, cores, None, None, None, None)
     dt2 = time.perf_counter() - t0
-    return {"value": n2 / dt2, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"lookups [0, {n2}) of {workload} ({n2 / inputs_x.lookups:.1%} of the batch), "
-                      f"{dt2:.2f} s on {cores} threads"}
+    k0 = {"value": n2 / dt2, "unit": UNIT,
+          "sample": f"lookups [0, {n2}) of {workload} ({n2 / inputs_x.lookups:.1%} of the batch), "
+                    f"{dt2:.2f} s on {cores} threads"}
+    _, k1 = cpu_k1(L, oin, sd, inputs_x.lookups, cores, budget_s * 0.6)
+    return {"value": k0["value"], "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": k0["sample"] + " (k0, the event loop)", "k0": k0, "k1": k1}
 
 
 # ------------------------------------------------------------- reference arm
@@ -226,6 +253,18 @@ def reference_arm(args, rank):
         run((s * per_step) % max(1, inp.lookups - per_step), per_step)
     t = time.perf_counter() - t0
     value = per_step * args.steps / t
+    # the reference's sorted CPU path (optimisation 1, Simulation.c:698-871),
+    # reported beside the event loop; the line's value stays the event loop's
+    if ref is not None:
+        ref.refh_event_k1.restype = C.c_ulonglong
+        ref.refh_event_k1.argtypes = [C.POINTER(oracle.Inputs), C.POINTER(oracle.SimData)]
+        t0 = time.perf_counter()
+        ref.refh_event_k1(C.byref(inp), sdp)
+        dt = time.perf_counter() - t0
+        k1 = {"value": inp.lookups / dt, "unit": UNIT,
+              "sample": f"all {inp.lookups} lookups in one call, {dt:.2f} s on {cores} threads"}
+    else:
+        _, k1 = cpu_k1(oracle.lib(), prob.inp, C.byref(prob.sd), inp.lookups, cores, 6.0)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -234,7 +273,9 @@ def reference_arm(args, rank):
         "config": {"workload": args.workload, "kernel": "openmp-threading event loop (k0)",
                    "sample_lookups_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": f"{per_step} consecutive lookups of {args.workload} per step"},
+                         "sample": f"{per_step} consecutive lookups of {args.workload} per step "
+                                   "(k0, the event loop)",
+                         "k1": k1},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -256,6 +297,8 @@ def main():
                     help="override gridpoints per nuclide (a smaller case of the workload, for profiling)")
     ap.add_argument("--buckets", type=int, default=0, help="batched: energy buckets per material")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the end-to-end measurement through xs_lookup_samples (host buffers)")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the forward+adjoint side measurement (xs_run_adjoint, device arrays)")
     ap.add_argument("--no-batched", action="store_true",
@@ -336,19 +379,24 @@ def main():
                            or last.hash == expected)
 
     # end to end through the C ABI with host buffers: samples in, macro_xs out
-    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
-    hE, hM = pin((N,), torch.float64), pin((N,), torch.int32)
-    ctx.sample_event(first, N, hE, hM)
-    hmacro, hidx = pin((N, 5), torch.float64), pin((N,), torch.uint8)
-    ekw = dict(kernel=args.kernel, arith=args.arith, tile=args.tile, buckets=args.buckets)
-    ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)  # warm
-    e2e_t = []
-    for _ in range(max(1, args.e2e_steps)):
-        t0 = time.perf_counter()
-        re = ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_ok = re.verification == last.verification
-    e2e_value = world * N / statistics.median(e2e_t)
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+        hE, hM = pin((N,), torch.float64), pin((N,), torch.int32)
+        ctx.sample_event(first, N, hE, hM)
+        hmacro, hidx = pin((N, 5), torch.float64), pin((N,), torch.uint8)
+        ekw = dict(kernel=args.kernel, arith=args.arith, tile=args.tile, buckets=args.buckets)
+        ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)  # warm
+        e2e_t = []
+        for _ in range(max(1, args.e2e_steps)):
+            t0 = time.perf_counter()
+            re = ctx.lookup_samples(hE, hM, macro_out=hmacro, max_idx_out=hidx, **ekw)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e = {"value": world * N / statistics.median(e2e_t), "unit": UNIT,
+               "h2d_bytes_per_step": N * 12, "d2h_bytes_per_step": N * 41 + 8,
+               "api": "xs_lookup_samples (host pinned)",
+               "verification_matches": bool(re.verification == last.verification)}
+        del hE, hM, hmacro, hidx
 
     # the other lookup kernel on the same workload and context (same hash)
     other = None
@@ -443,9 +491,7 @@ def main():
                       "peak_source": "2 FP64 ops per SM per clock x SMs x max SM clock",
                       "frac": value * 11 * nbar_of(inputs, problem) / fp64_peak}
                      if args.arith == "fast" and args.kernel == "plain" else None),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": N * 12,
-                    "d2h_bytes_per_step": N * 41 + 8, "api": "xs_lookup_samples (host pinned)",
-                    "verification_matches": bool(e2e_ok)},
+            "e2e": e2e,
             "gpu_launches": launches,
             "other_kernel": other,
             "forward_adjoint": adj,

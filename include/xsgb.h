@@ -256,11 +256,12 @@ xs_status xs_adjoint_samples(xs_ctx *ctx, const xs_run_opts *opts, const double 
 
 /* Autotuner (no reference counterpart).  Times, on a sample of up to 4M of
  * the context's event lookups, the plain kernel's tile sizes, the batched
- * kernel's energy buckets, the persistent kernels' blocks per SM and every
+ * kernel's energy buckets, the persistent kernels' blocks per SM, the lanes
+ * per fuel lookup, the chosen kernel's threads per block (128, 256, 512) and every
  * grid type the context can serve (it derives a 10,000-bin hash grid and the
  * nuclide grid's search keys on the device when missing; all grid types give
  * the same intervals), installs the fastest as the context's defaults and
- * returns it in *best (kernel, tile_lookups, energy_buckets).  With
+ * returns it in *best (kernel, tile_lookups, energy_buckets, block_threads).  With
  * cache_path non-NULL the choice is read from, or merged into, a JSON file
  * keyed by (device name, problem), and a cached choice is installed without
  * timing. */
@@ -278,13 +279,19 @@ int xs_ctx_grid_type(const xs_ctx *ctx);
  * loading this library holds until exit; so it takes at most 524,288 lookups
  * (count) and 4,096 energy buckets per call (larger values are rejected with
  * XS_ERR_INVALID_ARGUMENT), and it calls no allocating routine.
- * Outputs (macro_xs_out count*5, max_idx_out count) must be device memory or
- * NULL; *verification (host) receives the un-modded sum; the call is ordered
- * on `stream` (NULL: the context's stream) and returns when it is done.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * All calls share the one array: calls whose work overlaps on the GPU (other
- * streams, other host threads) race on it and must be serialised by the caller. */
+ * energy_buckets <= 0 takes the context's batched bucket count, capped at 4,096.
+ * Outputs (macro_xs_out count*5, max_idx_out count) must be NULL or device
+ * memory of the context's device (or managed memory); *verification (host)
+ * receives the un-modded sum; the call is ordered on `stream` (NULL: the
+ * context's stream) and returns when it is done.  It runs on the context's
+ * device and leaves the calling thread's current device as it found it.
+ * The first call on a device (and the first after that device's CUDA context
+ * was re-created, e.g. by a cudaDeviceReset) looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the one array, which keeps the last call's
+ * contents (each call clears its counters and histogram first): calls whose
+ * work overlaps on the GPU (other streams, other host threads) race on it and
+ * must be serialised by the caller. */
 xs_status xs_run_event_batched_static(xs_ctx *ctx, long first, long count, int arith,
                                       int energy_buckets, double *macro_xs_out,
                                       unsigned char *max_idx_out, void *stream,

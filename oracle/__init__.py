@@ -22,6 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libxsref.so")
 REF_EXE_PATH = os.path.join(HERE, "_ref", "XSBench")
+# The reference checkout whose sources oracle/Makefile compiles into oracle/_ref
+# (the one setting for its location; XSBENCH_REFERENCE_DIR overrides it).
+REFERENCE_DIR = os.environ.get("XSBENCH_REFERENCE_DIR", "/root/reference")
 
 UNIONIZED, NUCLIDE, HASH = 0, 1, 2          # XSbench_header.h:37-39
 HISTORY_BASED, EVENT_BASED = 1, 2           # XSbench_header.h:42-43
@@ -93,9 +96,50 @@ class Config:
                       simulation_method=method, binary_mode=0, kernel_id=0)
 
 
+def datafile_digest(path: str) -> tuple:
+    """(length, sha256) of a dataset file in the format of binary_write
+    (openmp-threading/io.c:456-474: the raw SimulationData struct, then
+    num_nucs, concs, mats, nuclide_grid, index_grid, unionized_energy_array)
+    with the bytes the reference leaves undefined zeroed: the struct's pointer
+    fields (stale addresses) and its unused sample fields and padding (bytes
+    0-48 and 80-112), and the row padding of the 12 x max_num_nucs concs and
+    mats tables past each material's num_nucs entries (Materials.c mallocs the
+    tables and fills only those)."""
+    import hashlib
+    import struct
+    b = bytearray(open(path, "rb").read())
+    n_nn, n_concs, n_mats = struct.unpack_from("<3i", b, 48)
+    max_nucs = struct.unpack_from("<i", b, 76)[0]
+    b[0:48] = bytes(48)
+    b[80:112] = bytes(32)
+    nn = struct.unpack_from(f"<{n_nn}i", b, 112)
+    concs_at = 112 + 4 * n_nn
+    mats_at = concs_at + 8 * n_concs
+    for m, k in enumerate(nn):
+        row_end = (m + 1) * max_nucs
+        for j in range(m * max_nucs + k, min(row_end, n_concs)):
+            b[concs_at + 8 * j:concs_at + 8 * j + 8] = bytes(8)
+        for j in range(m * max_nucs + k, min(row_end, n_mats)):
+            b[mats_at + 4 * j:mats_at + 4 * j + 4] = bytes(4)
+    return len(b), hashlib.sha256(bytes(b)).hexdigest()
+
+
 def build() -> None:
-    """Compile liboracle.so (and, where the reference sources exist, oracle/_ref)."""
+    """Compile liboracle.so."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+
+
+def build_reference(cuda: bool = True) -> bool:
+    """Compile the reference's own sources where they lie under REFERENCE_DIR
+    into oracle/_ref (its openmp-threading build and, with `cuda`, its
+    cuda/Simulation.cu as an sm_103a cubin).  Returns False, building
+    nothing, where the reference is absent."""
+    if not os.path.isdir(os.path.join(REFERENCE_DIR, "openmp-threading")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_DIR}"], check=True)
+    if cuda and os.path.isdir(os.path.join(REFERENCE_DIR, "cuda")):
+        subprocess.run(["make", "-s", "-C", HERE, "refcuda", f"REF={REFERENCE_DIR}"], check=True)
+    return True
 
 
 _lib = None
@@ -116,6 +160,9 @@ def lib() -> C.CDLL:
         L.or_run_event.argtypes = [P(Inputs), P(SimData), C.c_long, C.c_long, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.or_run_event.restype = C.c_ulonglong
+        L.or_run_event_k1.argtypes = [P(Inputs), P(SimData), C.c_long, C.c_long, C.c_int,
+                                      C.c_void_p]
+        L.or_run_event_k1.restype = C.c_ulonglong
         L.or_run_event_samples.argtypes = [P(Inputs), P(SimData), C.c_long, C.c_void_p,
                                            C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.or_run_event_samples.restype = C.c_ulonglong

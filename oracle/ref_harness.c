@@ -11,6 +11,8 @@
  *                             (openmp-threading/Simulation.c:472,462,426,326)
  *   run_event_based_simulation / run_history_based_simulation
  *                             (openmp-threading/Simulation.c:15,116)
+ *   run_event_based_simulation_optimization_1
+ *                             (openmp-threading/Simulation.c:698)
  */
 #include "XSbench_header.h"
 
@@ -63,6 +65,12 @@ unsigned long long refh_run_event(Inputs *in, SimulationData *sd, long first, lo
 unsigned long long refh_event_simulation(Inputs *in, SimulationData *sd)
 {
     return run_event_based_simulation(*in, *sd, 1);
+}
+
+/* Optimisation 1 (Simulation.c:698-871) over in->lookups lookups. */
+unsigned long long refh_event_k1(Inputs *in, SimulationData *sd)
+{
+    return run_event_based_simulation_optimization_1(*in, *sd, 1);
 }
 
 unsigned long long refh_history_simulation(Inputs *in, SimulationData *sd)

@@ -13,6 +13,7 @@
 
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -174,6 +175,13 @@ int or_argmax5(const double macro[5])
     return arg;
 }
 
+static double or_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 static void or_set_threads(int nthreads)
 {
 #ifdef _OPENMP
@@ -221,6 +229,139 @@ unsigned long long or_run_event_samples(const or_inputs *in, const or_simdata *s
         if (macro_out) memcpy(&macro_out[t * 5], macro, sizeof macro);
         if (maxidx_out) maxidx_out[t] = (unsigned char)arg;
     }
+    return verification;
+}
+
+/* ---------------------------------------------- optimisation 1 (k1) --- */
+/* Simulation.c:698-871: the sampling loop split from the lookups, the samples
+ * sorted by material and then, within each material, by energy, and the
+ * lookups run material by material.  The two sorts are parallel quicksorts
+ * of (key, payload) pairs, as the reference's are (Simulation.c:565-688:
+ * recursion into OpenMP tasks above 10,000 entries, at most 16 threads); the
+ * one below is this oracle's own, a Hoare partition around the middle entry. */
+
+#define OR_SORT_TASK_CUTOFF 10000
+
+/* sort (mat key, energy payload) by material */
+static void or_qsort_mat(int *key, double *val, long lo, long hi)
+{
+    while (lo < hi) {
+        const int pivot = key[lo + (hi - lo) / 2];
+        long a = lo, b = hi;
+        while (a <= b) {
+            while (key[a] < pivot) a++;
+            while (key[b] > pivot) b--;
+            if (a <= b) {
+                int tk = key[a]; key[a] = key[b]; key[b] = tk;
+                double tv = val[a]; val[a] = val[b]; val[b] = tv;
+                a++;
+                b--;
+            }
+        }
+        if (hi - lo >= OR_SORT_TASK_CUTOFF) {
+#pragma omp task
+            or_qsort_mat(key, val, lo, b);
+#pragma omp task
+            or_qsort_mat(key, val, a, hi);
+            return;
+        }
+        if (b - lo < hi - a) {     /* recurse into the shorter side */
+            or_qsort_mat(key, val, lo, b);
+            lo = a;
+        } else {
+            or_qsort_mat(key, val, a, hi);
+            hi = b;
+        }
+    }
+}
+
+/* sort (energy key, mat payload) by energy */
+static void or_qsort_energy(double *key, int *val, long lo, long hi)
+{
+    while (lo < hi) {
+        const double pivot = key[lo + (hi - lo) / 2];
+        long a = lo, b = hi;
+        while (a <= b) {
+            while (key[a] < pivot) a++;
+            while (key[b] > pivot) b--;
+            if (a <= b) {
+                double tk = key[a]; key[a] = key[b]; key[b] = tk;
+                int tv = val[a]; val[a] = val[b]; val[b] = tv;
+                a++;
+                b--;
+            }
+        }
+        if (hi - lo >= OR_SORT_TASK_CUTOFF) {
+#pragma omp task
+            or_qsort_energy(key, val, lo, b);
+#pragma omp task
+            or_qsort_energy(key, val, a, hi);
+            return;
+        }
+        if (b - lo < hi - a) {
+            or_qsort_energy(key, val, lo, b);
+            lo = a;
+        } else {
+            or_qsort_energy(key, val, a, hi);
+            hi = b;
+        }
+    }
+}
+
+static int or_sort_threads(int nthreads)
+{
+    return nthreads > 16 ? 16 : (nthreads > 0 ? nthreads : 1);   /* Simulation.c:612-613 */
+}
+
+unsigned long long or_run_event_k1(const or_inputs *in, const or_simdata *sd, long first, long n,
+                                   int nthreads, double phase_s[4])
+{
+    double *E = (double *)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+    int *M = (int *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+    unsigned long long verification = 0;
+    if (!E || !M) {
+        free(E);
+        free(M);
+        return 0;
+    }
+    or_set_threads(nthreads);
+    double t0 = or_now();
+#pragma omp parallel for schedule(dynamic, 100)
+    for (long t = 0; t < n; t++) or_sample_event(first + t, &E[t], &M[t]);
+    double t1 = or_now();
+#pragma omp parallel num_threads(or_sort_threads(nthreads))
+    {
+#pragma omp single nowait
+        if (n > 1) or_qsort_mat(M, E, 0, n - 1);
+    }
+    long count[12] = {0}, offset[12] = {0};
+    for (long t = 0; t < n; t++) count[M[t]]++;
+    for (int m = 1; m < 12; m++) offset[m] = offset[m - 1] + count[m - 1];
+    for (int m = 0; m < 12; m++) {
+#pragma omp parallel num_threads(or_sort_threads(nthreads))
+        {
+#pragma omp single nowait
+            if (count[m] > 1) or_qsort_energy(E + offset[m], M + offset[m], 0, count[m] - 1);
+        }
+    }
+    double t2 = or_now();
+    for (int m = 0; m < 12; m++) {
+#pragma omp parallel for schedule(dynamic, 100) reduction(+ : verification)
+        for (long t = offset[m]; t < offset[m] + count[m]; t++) {
+            double macro[5];
+            or_macro_xs(in, sd, E[t], M[t], macro);
+            verification += (unsigned long long)(or_argmax5(macro) + 1);
+        }
+    }
+    double t3 = or_now();
+    if (phase_s) {
+        phase_s[0] = t1 - t0;   /* sampling */
+        phase_s[1] = t2 - t1;   /* material and energy sorts */
+        phase_s[2] = t3 - t2;   /* lookups */
+        phase_s[3] = t3 - t0;
+    }
+    free(E);
+    free(M);
     return verification;
 }
 

@@ -97,6 +97,12 @@ unsigned long long or_run_event(const or_inputs *in, const or_simdata *sd, long 
                                 double *energy_out, int *mat_out);
 
 /* Event lookups with caller-supplied (energy, material) samples. */
+/* Optimisation 1 (Simulation.c:698-871) over lookups [first, first+n): sample,
+ * sort by material then by energy, look up material by material.  The same
+ * verification sum as or_run_event.  phase_s (nullable) receives the seconds
+ * of sampling, sorting, lookups and the total. */
+unsigned long long or_run_event_k1(const or_inputs *in, const or_simdata *sd, long first, long n,
+                                   int nthreads, double phase_s[4]);
 unsigned long long or_run_event_samples(const or_inputs *in, const or_simdata *sd, long n,
                                         const double *energy, const int *mat, int nthreads,
                                         double *macro_out, unsigned char *maxidx_out);

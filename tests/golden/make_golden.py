@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = "/root/reference/openmp-threading"
+REF_DIR = os.path.join(oracle.REFERENCE_DIR, "openmp-threading")
 
 
 def sha(a: np.ndarray) -> str:
@@ -50,8 +50,8 @@ def sha(a: np.ndarray) -> str:
 
 
 def ref_lib() -> C.CDLL:
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={REF_DIR}"],
-                   check=True)
+    if not oracle.build_reference(cuda=False):
+        raise SystemExit(f"the reference checkout is missing: {oracle.REFERENCE_DIR}")
     L = C.CDLL(oracle.REF_LIB_PATH)
     P = C.POINTER
     L.refh_grid_init.argtypes = [P(oracle.Inputs)]
@@ -186,6 +186,34 @@ def layout():
     print("[layout]", rec, flush=True)
 
 
+# The dataset file of binary_write (openmp-threading/io.c:456-474), digested
+# with the bytes the reference leaves undefined zeroed (oracle.datafile_digest).
+DATAFILE_CASES = {
+    "tiny_unionized": ["-s", "small", "-g", "1000", "-G", "unionized"],
+    "tiny_hash": ["-s", "small", "-g", "1000", "-G", "hash", "-h", "500"],
+    "small_unionized": ["-s", "small", "-G", "unionized"],
+}
+
+
+def datafile():
+    """Digests of the dataset files the reference's own binary_write makes
+    (oracle/_ref/XSBench ... -b write, in a scratch directory)."""
+    import tempfile
+    rec = {}
+    for name, args in DATAFILE_CASES.items():
+        with tempfile.TemporaryDirectory() as d:
+            # exit status 1 = "invalid checksum" for the reduced problems (no
+            # published value); the file is written before the lookups run
+            out = subprocess.run([oracle.REF_EXE_PATH, *args, "-m", "event", "-l", "1000",
+                                  "-t", "1", "-b", "write"], cwd=d, capture_output=True, text=True)
+            assert "Writing all data structures" in out.stdout, out.stdout + out.stderr
+            n, h = oracle.datafile_digest(os.path.join(d, "XS_data.dat"))
+        rec[name] = {"args": args, "bytes": n, "sha256_masked": h}
+        print("[datafile]", name, n, h, flush=True)
+    with open(os.path.join(OUT, "datafile.json"), "w") as f:
+        json.dump(rec, f, indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--xl", action="store_true", help="also the XL hash-grid config (slow)")
@@ -193,6 +221,10 @@ def main():
     args = ap.parse_args()
     if args.only == "layout":
         layout()
+        return
+    if args.only == "datafile":
+        ref_lib()   # builds oracle/_ref
+        datafile()
         return
     L = ref_lib()
     L.refh_set_threads(os.cpu_count() or 1)
@@ -216,6 +248,7 @@ def main():
         one_config(L, name, cfg)
     if not args.only:
         layout()
+        datafile()
         history(L, "small")
         history(L, "large")
 

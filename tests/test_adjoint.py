@@ -4,8 +4,12 @@ Bars: every gradient array within 1e-8 relative (max norm over the array,
 max|a - b| / max|b|) of the plain-PyTorch FP64 reference gradient
 (tests/torch_reference.py) and of central finite differences (h = 1e-6) of
 the oracle's forward; bit-identical results on repeated runs.  Sizes: 68
-nuclides x 1000 gridpoints, 100,000 lookups; the full-size run is checked
-through linearity (the gradient of a split batch adds up).
+nuclides x 1000 gridpoints, 100,000 lookups; the forward + adjoint
+configuration of the benchmark (68 nuclides x 11,303 gridpoints, 100,000
+lookups, all three grids) against both; the full-size problem (355 x 11,303,
+17M lookups, unionized grid with its union table and hash grid) on 20,000
+lookups spread over the batch, and through linearity (the gradient of a split
+batch adds up).
 """
 import numpy as np
 import pytest
@@ -21,6 +25,12 @@ TOL = 1e-8
 
 def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def rel_rows(a, b):
+    """Largest per-lookup relative difference of macro_xs vectors (max norm)."""
+    num = np.max(np.abs(a - b), axis=1)
+    return float(np.max(num / np.maximum(np.max(np.abs(b), axis=1), 1e-300)))
 
 
 def fd_tol(ad, lp, lm, h):
@@ -155,20 +165,13 @@ def test_adjoint_repeated_energies(ctxs, name):
     assert rel(d_x, ref_x) <= TOL
 
 
-@pytest.mark.gpu
-def test_adjoint_against_central_differences(ctxs):
-    """FD (h = 1e-6) of the oracle's forward, on per-lookup functionals."""
-    prob, ctx = ctx_for(ctxs, "tiny_unionized")
-    n = 20000
-    g = gbar_for(n, seed=11)
-    d_e = np.empty(n)
-    d_c = np.zeros((12, 34))
-    d_x = np.zeros((68, 1000, 5))
-    ctx.adjoint(g, count=n, d_concs=d_c, d_xs=d_x, d_energy=d_e)
-    E, M = ctx.sample_event(0, n)
+def check_central_differences(ctx, name, n_gp, max_nucs, n, d_c, d_x, d_e, g, E, M):
+    """Central differences (h = 1e-6) of the oracle's forward on per-lookup
+    functionals against the adjoint's d_concs, d_xs and d_energy of lookups
+    (E, M) with upstream gradients g."""
     h = 1e-6
-    with oracle.Problem(oracle_config("tiny_unionized")) as o:
-        egrid = o.arrays()["nuclide_grid"].reshape(68, 1000, 6)[:, :, 0]
+    with oracle.Problem(oracle_config(name)) as o:
+        egrid = o.arrays()["nuclide_grid"].reshape(68, n_gp, 6)[:, :, 0]
 
         def L(sel, energies=None):
             e = E[sel] if energies is None else energies
@@ -179,7 +182,7 @@ def test_adjoint_against_central_differences(ctxs):
         for m, j in ((0, 0), (0, 33), (2, 1), (4, 26), (11, 8)):
             sel = np.nonzero(M == m)[0]
             p = o.sd.concs
-            idx = m * 34 + j
+            idx = m * max_nucs + j
             c0 = p[idx]
             p[idx] = c0 + h
             lp = L(sel)
@@ -191,22 +194,22 @@ def test_adjoint_against_central_differences(ctxs):
 
         # tabulated xs: restrict L to the lookups near the perturbed gridpoint
         grid = o.sd.nuclide_grid
-        for nuc, pt, ch in ((58, 500, 0), (24, 10, 3), (63, 998, 4), (41, 1, 1)):
+        for nuc, pt, ch in ((58, n_gp // 2, 0), (24, 10, 3), (63, n_gp - 2, 4), (41, 1, 1)):
             lo_e = egrid[nuc][max(pt - 1, 0)]
-            hi_e = egrid[nuc][min(pt + 1, 999)]
+            hi_e = egrid[nuc][min(pt + 1, n_gp - 1)]
             sel = np.nonzero((E >= lo_e) & (E <= hi_e))[0]
             if pt <= 1:
                 sel = np.nonzero(E <= hi_e)[0]
-            if pt >= 998:
+            if pt >= n_gp - 2:
                 sel = np.nonzero(E >= lo_e)[0]
             field = ("total_xs", "elastic_xs", "absorbtion_xs", "fission_xs", "nu_fission_xs")[ch]
-            gp = grid[nuc * 1000 + pt]
+            gp = grid[nuc * n_gp + pt]
             v0 = getattr(gp, field)
-            setattr(grid[nuc * 1000 + pt], field, v0 + h)
+            setattr(grid[nuc * n_gp + pt], field, v0 + h)
             lp = L(sel)
-            setattr(grid[nuc * 1000 + pt], field, v0 - h)
+            setattr(grid[nuc * n_gp + pt], field, v0 - h)
             lm = L(sel)
-            setattr(grid[nuc * 1000 + pt], field, v0)
+            setattr(grid[nuc * n_gp + pt], field, v0)
             fd = (lp - lm) / (2 * h)
             assert abs(fd - d_x[nuc, pt, ch]) <= fd_tol(d_x[nuc, pt, ch], lp, lm, h), (nuc, pt, ch)
 
@@ -230,6 +233,93 @@ def test_adjoint_against_central_differences(ctxs):
             if checked == 40:
                 break
         assert checked == 40
+
+
+@pytest.mark.gpu
+def test_adjoint_against_central_differences(ctxs):
+    """FD (h = 1e-6) of the oracle's forward, on per-lookup functionals."""
+    prob, ctx = ctx_for(ctxs, "tiny_unionized")
+    n = 20000
+    g = gbar_for(n, seed=11)
+    d_e = np.empty(n)
+    d_c = np.zeros((12, 34))
+    d_x = np.zeros((68, 1000, 5))
+    ctx.adjoint(g, count=n, d_concs=d_c, d_xs=d_x, d_energy=d_e)
+    E, M = ctx.sample_event(0, n)
+    check_central_differences(ctx, "tiny_unionized", 1000, 34, n, d_c, d_x, d_e, g, E, M)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["small_unionized", "small_hash", "small_nuclide"])
+def test_adjoint_benchmark_configuration_small(name):
+    """The forward + adjoint configuration at the size its check is defined
+    for: 68 nuclides x 11,303 gridpoints, 100,000 lookups of the event batch,
+    upstream gradients N(0,1); every gradient array and macro_xs against the
+    plain-PyTorch FP64 reference (1e-8 / 1e-12), and central differences of
+    the oracle's forward (h = 1e-6, bracket-safe energies)."""
+    inp = product_inputs(name)
+    n, n_gp = N, 11303
+    with X.grid_init(inp) as prob, X.Context(inp, prob) as ctx:
+        g = gbar_for(n, seed=29)
+        macro = np.empty((n, 5))
+        d_e = np.empty(n)
+        d_c = np.zeros((12, 34))
+        d_x = np.zeros((68, n_gp, 5))
+        r = ctx.adjoint(g, count=n, macro_out=macro, d_concs=d_c, d_xs=d_x, d_energy=d_e)
+        assert r.verification == ctx.run_event(count=n).verification
+        E, M = ctx.sample_event(0, n)
+        egrid, xs, concs, mats, nn = tables_from_arrays(prob.arrays(), 68, n_gp, 34)
+    ref_macro, ref_e, ref_c, ref_x = reference_gradients(E, M, g, egrid, xs, concs, mats, nn)
+    assert rel_rows(macro, ref_macro) <= 1e-12
+    assert rel(d_e, ref_e) <= TOL
+    assert rel(d_c, ref_c) <= TOL
+    assert rel(d_x, ref_x) <= TOL
+    check_central_differences(None, name, n_gp, 34, n, d_c, d_x, d_e, g, E, M)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["large_unionized", "large_hash"])
+def test_adjoint_full_size_against_torch_reference(name):
+    """The benchmarked forward + adjoint at full size: 355 nuclides x 11,303
+    gridpoints, 17M lookups.  On the unionized grid the context builds its
+    union table, and the adjoint's forward pass reads it, which is the path
+    the benchmark times.  (1) The whole batch through xs_run_adjoint on
+    device arrays: macro_xs and the energy gradient (per-lookup values) of
+    20,000 lookups spread over the batch against the torch reference.  (2)
+    Those 20,000 lookups as caller samples through xs_adjoint_samples (the
+    same kernels): all three gradient arrays against the torch reference."""
+    import torch
+    inp = product_inputs(name)
+    n_gp, mx = 11303, 321
+    with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
+        if name == "large_unionized":
+            assert ctx.union_table_bytes > 0
+        n = inp.lookups
+        g = gbar_for(n, seed=17)
+        dev = dict(dtype=torch.float64, device="cuda")
+        d_e, macro = torch.empty(n, **dev), torch.empty((n, 5), **dev)
+        d_c, d_x = torch.zeros((12, mx), **dev), torch.zeros((355, n_gp, 5), **dev)
+        r = ctx.adjoint(torch.from_numpy(g).cuda(), macro_out=macro, d_concs=d_c, d_xs=d_x,
+                        d_energy=d_e)
+        assert r.hash == X.EXPECTED_HASH[("event", "large")]
+        sel = np.linspace(0, n - 1, 20000).astype(np.int64)
+        d_e_sel = d_e.cpu().numpy()[sel]
+        macro_sel = macro.cpu().numpy()[sel]
+        del d_e, macro, d_c, d_x
+        E, M = ctx.sample_event(0, n)
+        Es, Ms, gs = E[sel].copy(), M[sel].copy(), np.ascontiguousarray(g[sel])
+        del E, M, g
+        m2, e2 = np.empty((sel.size, 5)), np.empty(sel.size)
+        c2, x2 = np.zeros((12, mx)), np.zeros((355, n_gp, 5))
+        ctx.adjoint(gs, energy=Es, mat=Ms, macro_out=m2, d_concs=c2, d_xs=x2, d_energy=e2)
+        egrid, xs, concs, mats, nn = tables_from_arrays(p.arrays(), 355, n_gp, mx)
+    ref_macro, ref_e, ref_c, ref_x = reference_gradients(Es, Ms, gs, egrid, xs, concs, mats, nn)
+    assert rel_rows(macro_sel, ref_macro) <= 1e-12
+    assert rel(d_e_sel, ref_e) <= TOL
+    assert rel_rows(m2, ref_macro) <= 1e-12
+    assert rel(e2, ref_e) <= TOL
+    assert rel(c2, ref_c) <= TOL
+    assert rel(x2, ref_x) <= TOL
 
 
 @pytest.mark.gpu

@@ -156,7 +156,9 @@ def test_xl_against_reference(name):
     """XL (355 x 238,847 points, 100M lookups).  The reference has no XL
     constant (io.c:85-106); the digests come from its own build.  The nuclide
     grid gives the same interval as the hash grid for every lookup, so both
-    are held to the hash-grid digests."""
+    are held to the hash-grid digests: EXACT bit for bit, FAST by the argmax
+    digest and 1e-12 of the EXACT macro_xs."""
+    import torch
     g = golden_json("full_xl_hash")
     gl = golden_npz("lookups_xl_hash")
     ctx = ctx_for(name)
@@ -166,10 +168,21 @@ def test_xl_against_reference(name):
     assert sha(i) == g["sha256_max_idx"]
     assert sha(m) == g["sha256_macro_xs"]
     assert np.array_equal(m[gl["index"]], gl["macro_xs"])
+    # FAST, both kernels: the whole argmax vector against the reference's
+    # digest, and every lookup's macro_xs vector within 1e-12 (max norm) of
+    # the EXACT (reference-identical) run, compared on the device
+    m_exact = torch.from_numpy(m).cuda()
     del m
+    den = m_exact.abs().amax(dim=1).clamp_min(1e-300)
     for kernel in ("plain", "batched"):
-        r = ctx.run_event(kernel=kernel, arith="fast")
+        md = torch.empty((n, 5), dtype=torch.float64, device="cuda")
+        idd = torch.empty(n, dtype=torch.uint8, device="cuda")
+        r = ctx.run_event(kernel=kernel, arith="fast", macro_out=md, max_idx_out=idd)
         assert r.verification == g["verification"], kernel
+        assert sha(idd.cpu().numpy()) == g["sha256_max_idx"], kernel
+        err = float(((md - m_exact).abs().amax(dim=1) / den).max())
+        assert err <= REL_TOL, (kernel, err)
+        del md, idd
 
 
 def test_verification_only_runs_match():
@@ -267,6 +280,25 @@ def test_history_full_published_hash(size):
                 r = ctx.run_history(kernel=kernel, arith=arith)
                 assert r.verification == g["verification"], (kernel, arith)
                 assert r.verification % 999983 == g["hash"]
+
+
+def test_c_driver_dataset_file_round_trip(tmp_path):
+    """The C host program writes the problem to XS_data.dat (-b write) and a
+    second run reads it back (-b read) instead of building it (Main.c:50-58);
+    both report the published hash, and the file is the reference's own
+    binary_write output for the problem (masked digest from the reference
+    build, io.c:456-474)."""
+    import subprocess
+    from xsbench_gb300 import build as B
+    args = ["-m", "event", "-s", "small", "-G", "unionized"]
+    for mode in ("write", "read"):
+        out = subprocess.run([B.EXE_PATH, *args, "-b", mode], cwd=str(tmp_path),
+                             capture_output=True, text=True, timeout=600)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "945990" in out.stdout, mode
+    rec = golden_json("datafile")["small_unionized"]
+    assert oracle.datafile_digest(str(tmp_path / "XS_data.dat")) == (rec["bytes"],
+                                                                      rec["sha256_masked"])
 
 
 @pytest.mark.parametrize("method,expect", [("event", 945990), ("history", 941535)])

@@ -32,9 +32,33 @@ def test_autotune_keeps_results_and_caches(tmp_path, name):
         assert "GB300" in key or "|grid=" in key
         assert val["lookups_per_s"] > 0
         assert val["fuel_lanes"] in (1, 2, 4)
+        assert val["block"] == best["block"] in (128, 256, 512)
         with X.Context(inp, p) as ctx2:
             t0 = time.perf_counter()
             best2 = ctx2.autotune(cache)
             assert time.perf_counter() - t0 < 5.0
             assert best2 == best
             assert ctx2.run_event(kernel=best2["kernel"]).verification == g["verification"]
+
+
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_every_block_shape_keeps_the_hash(block):
+    """The block shapes the tuner chooses among (threads per block of the
+    plain kernel and of the persistent list kernel, the threads per SM kept):
+    each gives the reference's verification sum and argmax vector."""
+    import numpy as np
+    from conftest import sha
+    name = "tiny_hash"
+    g = golden_json("full_" + name)
+    inp = product_inputs(name)
+    with X.grid_init(inp) as p, X.Context(inp, p) as ctx:
+        for kernel in ("plain", "batched"):
+            for arith in ("fast", "exact"):
+                idx = np.empty(g["lookups"], np.uint8)
+                r = ctx.run_event(kernel=kernel, arith=arith, block=block, max_idx_out=idx)
+                assert r.verification == g["verification"], (kernel, arith)
+                assert sha(idx) == g["sha256_max_idx"], (kernel, arith)
+        with pytest.raises(X.XSError):
+            ctx.run_event(block=64)
+        with pytest.raises(X.XSError):   # the plain kernel's block must divide its tile
+            ctx.run_event(block=512, tile=256)

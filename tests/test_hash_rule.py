@@ -66,3 +66,56 @@ def test_kernel_hash_rule_matches_reference():
         assert np.array_equal(ref, got), nuc
         checked += E.size
     assert checked > 10_000_000
+
+
+def guided_rule(g, guide, K, E, certain, ref):
+    """The plain kernel's guided search (macro_xs_guided): start at
+    clamp(guide[floor(E 2^K)] - 1, 0, n - 2), step up while E >= the
+    interval's upper energy; on the hash grid, `ref` where E is not certainly
+    inside its hash bin or equals the interval's lower gridpoint."""
+    n = g.shape[0]
+    b = np.floor(E * 2.0 ** K).astype(np.int64)
+    k = np.clip(guide[b] - 1, 0, n - 2)
+    while True:
+        step = (k < n - 2) & ~(E < g[np.minimum(k + 1, n - 1)])
+        if not step.any():
+            break
+        k = k + step
+    if certain is None:
+        return k
+    return np.where(~certain | (g[k] == E), ref, k)
+
+
+def test_guided_search_matches_reference():
+    """The guided search gives the reference's interval on the hash grid
+    (Simulation.c:273-301) and on the nuclide grid (:252-263) for the sampled
+    lookups and for energies on gridpoints, on and next to hash bin edges,
+    next to guide bin edges, and at 0."""
+    with oracle.Problem(oracle_config("tiny_hash")) as o:
+        a = {k: np.array(v) for k, v in o.arrays().items()}
+        r = o.run_event(want_samples=True)
+    n_iso, n_gp, bins = 68, 1000, 500
+    grid = a["nuclide_grid"].reshape(n_iso, n_gp, 6)[:, :, 0]
+    index = a["index_grid"].reshape(bins, n_iso)
+    du = 1.0 / bins
+    K = 12   # the guide size the context picks for 1,000 gridpoints: 2^(10 + 2) bins
+    rng = np.random.default_rng(11)
+    edges_k = np.arange(1, 2 ** K) / 2.0 ** K
+    extra = [grid.ravel()[rng.integers(0, grid.size, 4000)],
+             np.arange(bins) * du, np.nextafter(np.arange(1, bins) * du, 0.0),
+             np.nextafter(np.arange(bins) * du, 1.0), edges_k, np.nextafter(edges_k, 0.0),
+             np.array([0.0, np.nextafter(0.0, 1.0), np.nextafter(1.0, 0.0)])]
+    E = np.concatenate([r["energy"], *extra])
+    # xsgb_hash_bin's certainty: E * bins more than bins * 2^-50 from an integer
+    x = E.astype(np.longdouble) * bins
+    certain = (np.abs(x - np.rint(x)) > bins * 2.0 ** -50) & (E > 0)
+    b = np.clip((E / du).astype(np.int64), 0, bins - 1)
+    last = b == bins - 1
+    for nuc in range(n_iso):
+        g = grid[nuc]
+        guide = np.searchsorted(g, np.arange(2 ** K + 1) / 2.0 ** K, side="left")
+        ref_h = reference_hash_interval(g, index[b, nuc], index[np.minimum(b + 1, bins - 1), nuc],
+                                        last, E)
+        assert np.array_equal(guided_rule(g, guide, K, E, certain, ref_h), ref_h), nuc
+        ref_n = np.clip(np.searchsorted(g, E, side="right") - 1, 0, n_gp - 2)
+        assert np.array_equal(guided_rule(g, guide, K, E, None, None), ref_n), nuc

@@ -81,3 +81,28 @@ def test_oracle_planted_mistake_is_caught():
             for i, mx, m in zip(ref["index"][sel], ref["macro_xs"][sel], ref["mat"][sel]) if m == 0]
     assert any(diff)
     assert g["lookups"] == 200000
+
+
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "tiny_nuclide", "small_hash"])
+def test_oracle_optimisation_1_port(name):
+    """The port of the reference's optimisation 1 (Simulation.c:698-871:
+    sampling split from the lookups, sorts by material and energy) gives the
+    reference's verification sum, on every grid; where the reference build is
+    present, its own optimisation 1 gives the same sum."""
+    import ctypes as C
+    import os
+    g = golden_json("full_" + name)
+    cfg = oracle_config(name)
+    with oracle.Problem(cfg) as p:
+        L = oracle.lib()
+        ph = (C.c_double * 4)()
+        v = L.or_run_event_k1(C.byref(p.inp), C.byref(p.sd), 0, g["lookups"], 4, ph)
+        assert v == g["verification"]
+        assert ph[3] > 0
+        if os.path.exists(oracle.REF_LIB_PATH) and name.startswith("tiny"):
+            ref = C.CDLL(oracle.REF_LIB_PATH)
+            ref.refh_event_k1.restype = C.c_ulonglong
+            ref.refh_event_k1.argtypes = [C.POINTER(oracle.Inputs), C.POINTER(oracle.SimData)]
+            inp = cfg.inputs()
+            inp.lookups = g["lookups"]
+            assert ref.refh_event_k1(C.byref(inp), C.byref(p.sd)) == g["verification"]

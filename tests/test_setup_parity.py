@@ -65,6 +65,66 @@ def test_binary_file_round_trip(tmp_path):
     assert sz == expect
 
 
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash", "small_unionized"])
+def test_binary_write_matches_reference_writer(tmp_path, name):
+    """xs_binary_write writes, byte for byte, the file the reference's own
+    binary_write writes for the same problem (openmp-threading/io.c:456-474;
+    digest from the reference build, tests/golden/make_golden.py), apart from
+    the struct's pointer fields and unused sample fields, which the reference
+    dumps as stale addresses and uninitialised memory, and the unfilled row
+    padding of its concs and mats tables (oracle.datafile_digest)."""
+    g = golden_json("datafile")
+    rec = g[name]
+    path = str(tmp_path / "XS_data.dat")
+    inp = X.read_cli(rec["args"] + ["-m", "event"])
+    with X.grid_init(inp) as p:
+        p.write(path)
+    assert oracle.datafile_digest(path) == (rec["bytes"], rec["sha256_masked"])
+
+
+def reference_exe():
+    if not os.path.exists(oracle.REF_EXE_PATH):
+        pytest.skip("the reference build (oracle/_ref) is not present on this machine")
+    return oracle.REF_EXE_PATH
+
+
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_hash"])
+def test_binary_read_of_reference_written_file(tmp_path, name):
+    """A file written by the reference build itself is read by xs_binary_read
+    into arrays identical to the reference's setup (sha256 of every array),
+    and its masked digest is the committed one."""
+    import subprocess
+    g = golden_json("datafile")
+    rec = g[name]
+    subprocess.run([reference_exe(), *rec["args"], "-m", "event", "-l", "1000", "-t", "2",
+                    "-b", "write"], cwd=str(tmp_path), capture_output=True, timeout=600)
+    path = str(tmp_path / "XS_data.dat")
+    assert oracle.datafile_digest(path) == (rec["bytes"], rec["sha256_masked"])
+    setup = golden_json("setup_" + name)
+    with X.HostProblem.from_file(product_inputs(name), path) as q:
+        for k, v in q.arrays().items():
+            assert sha(v) == setup["sha256"][k], k
+
+
+def test_reference_reads_file_written_here(tmp_path):
+    """The reference build reads a file written by xs_binary_write
+    (binary_read, io.c:476-508) and its lookups give the reference's
+    verification value for that problem."""
+    import re
+    import subprocess
+    exe = reference_exe()
+    name = "tiny_unionized"
+    full = golden_json("full_" + name)
+    with X.grid_init(product_inputs(name)) as p:
+        p.write(str(tmp_path / "XS_data.dat"))
+    out = subprocess.run([exe, "-s", "small", "-g", "1000", "-G", "unionized", "-m", "event",
+                          "-l", str(full["lookups"]), "-t", "4", "-b", "read"],
+                         cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+    assert "Reading all data structures" in out.stdout
+    m = re.search(r"Verification checksum: (\d+)", out.stdout)
+    assert m and int(m.group(1)) == full["hash"], out.stdout[-500:]
+
+
 def test_binary_read_rejects_garbage(tmp_path):
     path = tmp_path / "bad.dat"
     path.write_bytes(b"\x01" * 64)

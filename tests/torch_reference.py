@@ -38,6 +38,9 @@ def macro_xs(E, mat, concs, xs, egrid, mats, num_nucs):
     n_gp = egrid.shape[1]
     out = torch.zeros((n, 5), dtype=torch.float64)
     e_np = E.detach().numpy()
+    # one view per nuclide: the backward of each gather is then one nuclide's
+    # [n_gp, 5] block instead of a dense copy of the whole table
+    xs_n = xs.unbind(0)
     for m in range(12):
         rows = np.nonzero(mat == m)[0]
         if rows.size == 0:
@@ -52,8 +55,8 @@ def macro_xs(E, mat, concs, xs, egrid, mats, num_nucs):
             lo_e = torch.from_numpy(egrid[nuc][k])
             hi_e = torch.from_numpy(egrid[nuc][k + 1])
             f = (hi_e - Em) / (hi_e - lo_e)
-            lo = xs[nuc, kt]
-            hi = xs[nuc, kt + 1]
+            lo = xs_n[nuc][kt]
+            hi = xs_n[nuc][kt + 1]
             micro = hi - f[:, None] * (hi - lo)
             out = out.index_add(0, idx, micro * concs[m, j])
     return out

@@ -149,6 +149,35 @@ def _addr(x):
     raise TypeError(f"unsupported array type {type(x)}")
 
 
+_DTYPES = {"f64": (np.float64, "float64"), "i32": (np.int32, "int32"), "u8": (np.uint8, "uint8")}
+
+
+def _check_array(x, n_elems: int, kind: str, name: str, device: bool | None = None):
+    """Raises ValueError unless x is None or a contiguous array of n_elems
+    elements of type `kind` ("f64", "i32", "u8"); device=True / False also
+    requires a CUDA tensor / host array.  The C side receives bare pointers
+    and cannot check sizes, so this is where a short or mistyped buffer is
+    caught before a kernel writes past its end."""
+    if x is None:
+        return
+    np_t, torch_name = _DTYPES[kind]
+    if isinstance(x, np.ndarray):
+        ok_type, numel, is_dev = x.dtype == np_t, int(x.size), False
+    elif hasattr(x, "data_ptr"):
+        ok_type = str(x.dtype).replace("torch.", "") == torch_name
+        numel, is_dev = int(x.numel()), bool(getattr(x, "is_cuda", False))
+    else:
+        raise TypeError(f"{name}: unsupported array type {type(x)}")
+    if not ok_type:
+        raise ValueError(f"{name} must hold {torch_name} elements, not {x.dtype}")
+    if numel != int(n_elems):
+        raise ValueError(f"{name} must hold {int(n_elems)} elements, not {numel}")
+    if device is True and not is_dev:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if device is False and is_dev:
+        raise ValueError(f"{name} must be a host array")
+
+
 # ------------------------------------------------------------------ inputs
 def read_cli(args) -> Inputs:
     """Inputs from a reference-style command line (io.c:227-454)."""
@@ -262,13 +291,14 @@ class Result:
 
 
 def _opts(kernel=KERNEL_PLAIN, arith=ARITH_FAST, first=0, count=0, tile=0, buckets=0,
-          checked=False, async_=False, stream=None) -> RunOpts:
+          checked=False, async_=False, stream=None, block=0) -> RunOpts:
     o = RunOpts()
     lib().xs_run_opts_init(C.byref(o))
     o.kernel = {"plain": KERNEL_PLAIN, "batched": KERNEL_BATCHED}.get(kernel, kernel)
     o.arith = {"fast": ARITH_FAST, "exact": ARITH_EXACT}.get(arith, arith)
     o.first, o.count = int(first), int(count)
     o.tile_lookups, o.energy_buckets = int(tile), int(buckets)
+    o.block_threads = int(block)
     o.checked, o.async_ = int(bool(checked)), int(bool(async_))
     if stream is not None:
         o.stream = C.c_void_p(stream if isinstance(stream, int) else stream.cuda_stream)
@@ -281,6 +311,10 @@ class Context:
     def __init__(self, inputs: Inputs, problem: HostProblem | None = None, device: int = 0):
         self.inputs = inputs
         self._h = C.c_void_p()
+        # row length of the 12-row material tables (d_concs is 12 x this):
+        # the fuel's nuclide count, Materials.c:7-30
+        self.max_num_nucs = (int(problem.sd.max_num_nucs) if problem is not None
+                             else (34 if int(inputs.n_isotopes) == 68 else 321))
         if problem is None:
             _check(lib().xs_ctx_create_on_device(C.byref(inputs), int(device), C.byref(self._h)),
                    "xs_ctx_create_on_device")
@@ -298,7 +332,13 @@ class Context:
         interval records)."""
         return int(lib().xs_ctx_union_table_bytes(self._h))
 
+    def _count(self, first=0, count=0, **_):
+        return int(count) if int(count) > 0 else int(self.inputs.lookups) - int(first)
+
     def run_event(self, macro_out=None, max_idx_out=None, **kw) -> Result:
+        n = self._count(**kw)
+        _check_array(macro_out, n * 5, "f64", "macro_out")
+        _check_array(max_idx_out, n, "u8", "max_idx_out")
         o = _opts(**kw)
         r = RunResult()
         pm, _ = _addr(macro_out)
@@ -312,6 +352,10 @@ class Context:
             raise ValueError("energy and mat lengths differ")
         if macro_out is not None and tuple(macro_out.shape) != (n, 5):
             raise ValueError("macro_out must be (n, 5)")
+        _check_array(energy, n, "f64", "energy")
+        _check_array(mat, n, "i32", "mat")
+        _check_array(macro_out, n * 5, "f64", "macro_out")
+        _check_array(max_idx_out, n, "u8", "max_idx_out")
         o = _opts(**kw)
         r = RunResult()
         pe, _ = _addr(energy)
@@ -328,6 +372,8 @@ class Context:
             energy_out = np.empty(int(count), np.float64)
         if mat_out is None:
             mat_out = np.empty(int(count), np.int32)
+        _check_array(energy_out, int(count), "f64", "energy_out")
+        _check_array(mat_out, int(count), "i32", "mat_out")
         pe, _ = _addr(energy_out)
         pm, _ = _addr(mat_out)
         _check(lib().xs_sample_event(self._h, int(first), int(count), pe, pm), "xs_sample_event")
@@ -344,10 +390,10 @@ class Context:
         """Batched lookups with no device allocation (at most 524,288 per call;
         outputs on the device or None); returns the un-modded verification sum."""
         v = C.c_ulonglong()
-        pm, dm = _addr(macro_out)
-        pi, di = _addr(max_idx_out)
-        if (pm and not dm) or (pi and not di):
-            raise ValueError("outputs must be device tensors")
+        _check_array(macro_out, int(count) * 5, "f64", "macro_out", device=True)
+        _check_array(max_idx_out, int(count), "u8", "max_idx_out", device=True)
+        pm, _ = _addr(macro_out)
+        pi, _ = _addr(max_idx_out)
         a = {"fast": ARITH_FAST, "exact": ARITH_EXACT}.get(arith, arith)
         s = None if stream is None else C.c_void_p(stream if isinstance(stream, int) else stream.cuda_stream)
         _check(lib().xs_run_event_batched_static(self._h, int(first), int(count), int(a),
@@ -361,6 +407,16 @@ class Context:
         (12 x max_num_nucs) and d_xs (n_isotopes x n_gridpoints x 5) are added
         to.  Lookups are [first, first+count) of the event batch, or the
         caller's (energy, mat) samples."""
+        n = int(energy.shape[0]) if energy is not None else self._count(**kw)
+        if energy is not None:
+            _check_array(energy, n, "f64", "energy")
+            _check_array(mat, n, "i32", "mat")
+        _check_array(gbar, n * 5, "f64", "gbar")
+        _check_array(macro_out, n * 5, "f64", "macro_out")
+        _check_array(d_concs, 12 * int(self.max_num_nucs), "f64", "d_concs")
+        _check_array(d_xs, int(self.inputs.n_isotopes) * int(self.inputs.n_gridpoints) * 5, "f64",
+                     "d_xs")
+        _check_array(d_energy, n, "f64", "d_energy")
         o = _opts(**kw)
         r = RunResult()
         a = [_addr(x)[0] for x in (gbar, macro_out, d_concs, d_xs, d_energy)]
@@ -380,7 +436,7 @@ class Context:
         _check(lib().xs_autotune(self._h, cache_path.encode() if cache_path else None,
                                  C.byref(o)), "xs_autotune")
         return {"kernel": ("plain", "batched")[o.kernel], "tile": o.tile_lookups,
-                "buckets": o.energy_buckets, "grid": self.grid_type}
+                "buckets": o.energy_buckets, "block": o.block_threads, "grid": self.grid_type}
 
     @property
     def grid_type(self) -> str:

@@ -704,6 +704,7 @@ xs_status launch_adjoint(xs_ctx *ctx, cudaStream_t st, long first, long count,
     l.fuel_lanes = 1;
     l.table = 1;   // the forward reads the union table when there is one
     l.sorted = 1;
+    l.block = 256;
     s = launch_adjoint_energy(ctx, st, l, gbar, sg, d_energy);
     if (s != XS_OK) return s;
 

@@ -135,8 +135,10 @@ static xs_status resolve(const xs_ctx *ctx, const xs_run_opts *o, long total, xs
     if (r->count <= 0) return fail(XS_ERR_INVALID_ARGUMENT, "no lookups in range");
     if (r->tile_lookups <= 0) r->tile_lookups = ctx->plain_tile;
     if (r->energy_buckets <= 0) r->energy_buckets = ctx->batched_buckets;
-    if (r->block_threads != 0 && r->block_threads != 256)
-        return fail(XS_ERR_INVALID_ARGUMENT, "block_threads %d: the lookup kernels run 256 threads per block", r->block_threads);
+    if (r->block_threads != 0 && r->block_threads != 128 && r->block_threads != 256 &&
+        r->block_threads != 512)
+        return fail(XS_ERR_INVALID_ARGUMENT, "block_threads %d: 0 (tuned), 128, 256 or 512",
+                    r->block_threads);
     return XS_OK;
 }
 
@@ -542,9 +544,11 @@ static xs_status run_once(xs_ctx *ctx, const xs_run_opts &o, const SampleInput &
             ps = carve_plain_scratch(ctx->s.plain_buf, n, o.tile_lookups);
             psp = &ps;
         }
-        s = launch_plain(ctx, st, o.arith, o.checked, o.first, n, o.tile_lookups, in, out, psp, &launches);
+        s = launch_plain(ctx, st, o.arith, o.checked, o.first, n, o.tile_lookups, o.block_threads,
+                         in, out, psp, &launches);
     } else
-        s = launch_batched(ctx, st, o.arith, o.checked, o.first, n, 256, o.energy_buckets, in, out, &launches);
+        s = launch_batched(ctx, st, o.arith, o.checked, o.first, n, o.block_threads,
+                           o.energy_buckets, in, out, &launches);
     if (s != XS_OK) return s;
     XS_CUDA(cudaEventRecord(ctx->ev1, st));
     ctx->last_stream = st;
@@ -639,13 +643,14 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         out.max_idx = dIdx;
         xs_status s;
         if (o.kernel == XS_KERNEL_PLAIN) {
-            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, in, out, nullptr,
-                             &launches);
+            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, o.block_threads, in,
+                             out, nullptr, &launches);
         } else {
             BatchedScratch bs = carve_batched_scratch(b + io_bytes, chunk, nb_log2);
             bs.verification = ctx->s.verification;
             bs.error = ctx->s.error;
-            s = enqueue_batched_buf(ctx, st, o.arith, o.checked, 0, m, nb_log2, in, out, bs, &launches);
+            s = enqueue_batched_buf(ctx, st, o.arith, o.checked, 0, m, nb_log2, o.block_threads, in,
+                                    out, bs, &launches);
         }
         if (s != XS_OK) return s;
         if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));

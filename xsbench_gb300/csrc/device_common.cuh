@@ -625,6 +625,221 @@ __device__ __forceinline__ void macro_xs_nuclide_warp(const Tables &t, double E,
     }
 }
 
+// ------------------------------------------------- guided interval search ---
+// The hash and nuclide grids both give nuclide nuc the interval
+// k = clamp(#{E_j <= E} - 1, 0, n_gp - 2) (Simulation.c:252-263; the hash grid's
+// exceptions are below).  The guide (Tables::guide) holds
+// g = #{E_j < b 2^-K} for the bin b = floor(E 2^K) of E, so the interval is
+// k = clamp(g - 1 + #{j >= g : E_j <= E}, 0, n_gp - 2); with about four bins
+// per gridpoint most bins hold no gridpoint and the count is 0.  The lookup
+// starts at k = clamp(g - 1, 0, n_gp - 2) -- E_k < b 2^-K <= E, so k is not
+// past the interval -- reads interval k's 96 bytes (FAST: its record; EXACT:
+// its two gridpoints), whose upper energy says whether E lies below it, and
+// steps up while E >= E_{k+1}: one guide entry and, for ~90 % of the
+// nuclides, one interval read, where a binary search makes ~14-18 dependent
+// reads.
+//
+// HASH (Simulation.c:273-302): for E strictly inside its hash bin
+// (xsgb_hash_bin certain, i.e. more than 2^-50 from both edges) the
+// reference's search gives the same k except by its edge rule
+// `E <= E[u_low] -> gridpoint 0`, which can then hold only if E equals a
+// gridpoint (the lower gridpoint of the interval found, E_k == E); that case
+// takes the reference's hash search (interval_hash).  E_high's rule
+// `E >= E[u_high] -> n_gp - 1` holds only when u_high = n_gp - 1, where the
+// clamp gives the same interval.
+//
+// Loads: the guide entries through L1-bypassing evict_first loads (the guide
+// of the XL grid is 1.5 GB, read at random); the interval through the same
+// loads and L2 policy as accumulate_fast / accumulate_exact.
+
+__device__ __forceinline__ int ld_guide(const int *p)
+{
+    int v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+                 : "=r"(v)
+                 : "l"(p), "l"(policy_first()));
+    return v;
+}
+
+// The 96 bytes of interval k: FAST, the record [E_hi, hi[5], slope[5], E_lo];
+// EXACT, the gridpoints k and k+1 [E_lo, lo[5], E_hi, hi[5]].
+template <int ARITH>
+__device__ __forceinline__ void load_interval(const Tables &t, int nuc, long k, double v[12])
+{
+    if (ARITH == XS_ARITH_EXACT) {
+        const double2 *g = reinterpret_cast<const double2 *>(t.grid + (long)nuc * t.n_gp + k);
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            const double2 x = ldg(g + i);
+            v[2 * i] = x.x;
+            v[2 * i + 1] = x.y;
+        }
+    } else {
+        const double *r = reinterpret_cast<const double *>(t.records + ((long)nuc * (t.n_gp - 1) + k) * kRecordPairs);
+        const unsigned long long pol = record_policy(t, nuc);
+        ld_v4(r, v[0], v[1], v[2], v[3], pol);
+        ld_v4(r + 4, v[4], v[5], v[6], v[7], pol);
+        ld_v4(r + 8, v[8], v[9], v[10], v[11], pol);
+    }
+}
+
+template <int ARITH>
+__device__ __forceinline__ double interval_e_hi(const double v[12])
+{
+    return ARITH == XS_ARITH_EXACT ? v[6] : v[0];
+}
+
+template <int ARITH>
+__device__ __forceinline__ double interval_e_lo(const double v[12])
+{
+    return ARITH == XS_ARITH_EXACT ? v[0] : v[11];
+}
+
+// accumulate_fast / accumulate_exact on an interval already loaded
+template <int ARITH, bool DE>
+__device__ __forceinline__ void accumulate_loaded(const double v[12], double E, double conc,
+                                                  double macro[5], double *S)
+{
+    if (ARITH == XS_ARITH_EXACT) {
+        const double f = __ddiv_rn(__dsub_rn(v[6], E), __dsub_rn(v[6], v[0]));
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+            double xs = __dsub_rn(v[7 + c], __dmul_rn(f, __dsub_rn(v[7 + c], v[1 + c])));
+            macro[c] = __dadd_rn(macro[c], __dmul_rn(xs, conc));
+        }
+    } else {
+        const double d = v[0] - E;
+#pragma unroll
+        for (int c = 0; c < 5; c++) macro[c] = fma(fma(-d, v[6 + c], v[1 + c]), conc, macro[c]);
+        if (DE) {
+#pragma unroll
+            for (int c = 0; c < 5; c++) S[c] = fma(conc, v[6 + c], S[c]);
+        }
+    }
+}
+
+// The lane's nuclides j = q0, q0 + stride, ... of the material through the
+// guide, software-pipelined like the unionized loop: the guide entry of
+// nuclide j+2 is loaded and interval j+1's first guess prefetched into L2
+// while nuclide j is interpolated.  Returns false, touching nothing, when E
+// is not eligible (outside [0, 1), NaN, or for HASH within 2^-50 of a hash bin
+// edge); the caller then runs its own search.
+template <int GRID, int ARITH, bool CHECKED, bool DE, bool SROW>
+__device__ __forceinline__ bool macro_xs_guided(const Tables &t, double E, int n, const int *mrow,
+                                                const double *crow, double macro[5], int *err,
+                                                double *S, int q0, int stride)
+{
+    const long long q = order_key(E);
+    if (!(q >= 0 && q < 0x3FF0000000000000LL)) return false;   // E in [0, 1)
+    long bin = 0;
+    if (GRID == XS_HASH && !xsgb_hash_bin(E, (uint32_t)t.hash_bins, t.hash_margin, &bin)) return false;
+    const int b = xsgb_floor_scaled_pow2(E, t.guide_log2);
+    const long gstride = (1L << t.guide_log2) + 1;
+    const int *gcol = t.guide + b;
+    const long top = t.n_gp - 2;
+    const int nl = n > q0 ? (n - q0 + stride - 1) / stride : 0;
+    mrow += q0;
+    crow += q0;
+    int gr[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) gr[i] = (i < nl) ? ld_guide(&gcol[(long)rd<SROW>(&mrow[i * stride]) * gstride]) : 0;
+    if (nl > 0) {
+        const long k0 = min(max((long)gr[0] - 1, 0L), top);
+        const int n0 = rd<SROW>(&mrow[0]);
+        prefetch_l2(interval_bytes<ARITH>(t, n0, k0), 96, prefetch_policy(t, n0));
+    }
+    for (int j0 = 0; j0 < nl; j0 += 2) {
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int j = j0 + i;
+            if (j < nl) {
+                long k = min(max((long)gr[i] - 1, 0L), top);
+                if (j + 2 < nl) gr[i] = ld_guide(&gcol[(long)rd<SROW>(&mrow[(j + 2) * stride]) * gstride]);
+                if (j + 1 < nl) {
+                    const long kp = min(max((long)gr[i ^ 1] - 1, 0L), top);
+                    const int np = rd<SROW>(&mrow[(j + 1) * stride]);
+                    prefetch_l2(interval_bytes<ARITH>(t, np, kp), 96, prefetch_policy(t, np));
+                }
+                const int nuc = rd<SROW>(&mrow[j * stride]);
+                const double conc = rd<SROW>(&crow[j * stride]);
+                double v[12];
+                load_interval<ARITH>(t, nuc, k, v);
+                while (k < top && !(E < interval_e_hi<ARITH>(v))) {
+                    k++;
+                    load_interval<ARITH>(t, nuc, k, v);
+                }
+                if (GRID == XS_HASH && interval_e_lo<ARITH>(v) == E) {
+                    // E on a gridpoint: the reference's own hash search and edge rule
+                    const long kh = interval_hash<CHECKED>(t, bin, nuc, q, err);
+                    if (kh != k) {
+                        k = kh;
+                        load_interval<ARITH>(t, nuc, k, v);
+                    }
+                }
+                accumulate_loaded<ARITH, DE>(v, E, conc, macro, S);
+            }
+        }
+    }
+    return true;
+}
+
+// The same intervals through the bin records (Tables::binrec, FAST): slot
+// (nuc, b) already holds the record of the interval the guided search starts
+// at, so the lane reads it at an address it knows without a load -- no
+// dependent read precedes the record -- and reads the guide and walks on only
+// when E lies at or past that interval's upper gridpoint (about one nuclide
+// in ten with four bins per gridpoint).  The bin records of the nuclides
+// t.bin_prefetch ahead are prefetched into L2.
+__device__ __forceinline__ const double *binrec_at(const Tables &t, int nuc, int b)
+{
+    return reinterpret_cast<const double *>(t.binrec + (((long)nuc << t.guide_log2) + b) * kRecordPairs);
+}
+
+template <int GRID, bool CHECKED, bool DE, bool SROW>
+__device__ __forceinline__ bool macro_xs_binned(const Tables &t, double E, int n, const int *mrow,
+                                                const double *crow, double macro[5], int *err,
+                                                double *S, int q0, int stride)
+{
+    const long long q = order_key(E);
+    if (!(q >= 0 && q < 0x3FF0000000000000LL)) return false;   // E in [0, 1)
+    long bin = 0;
+    if (GRID == XS_HASH && !xsgb_hash_bin(E, (uint32_t)t.hash_bins, t.hash_margin, &bin)) return false;
+    const int b = xsgb_floor_scaled_pow2(E, t.guide_log2);
+    const long top = t.n_gp - 2;
+    const int nl = n > q0 ? (n - q0 + stride - 1) / stride : 0;
+    mrow += q0;
+    crow += q0;
+    const int P = t.bin_prefetch;
+    const unsigned long long pol = policy_first();
+    for (int j = 0; j < P && j < nl; j++)
+        prefetch_l2(binrec_at(t, rd<SROW>(&mrow[j * stride]), b), 96, policy_last());
+#pragma unroll 2
+    for (int j = 0; j < nl; j++) {
+        if (j + P < nl) prefetch_l2(binrec_at(t, rd<SROW>(&mrow[(j + P) * stride]), b), 96, policy_last());
+        const int nuc = rd<SROW>(&mrow[j * stride]);
+        const double conc = rd<SROW>(&crow[j * stride]);
+        const double *r = binrec_at(t, nuc, b);
+        double v[12];
+        ld_v4(r, v[0], v[1], v[2], v[3], pol);
+        ld_v4(r + 4, v[4], v[5], v[6], v[7], pol);
+        ld_v4(r + 8, v[8], v[9], v[10], v[11], pol);
+        if (!(E < v[0])) {
+            // E at or past the bin's first interval: from there, through the guide
+            long k = min(max((long)ld_guide(&t.guide[(long)nuc * ((1L << t.guide_log2) + 1) + b]) - 1, 0L), top);
+            while (k < top && !(E < v[0])) {
+                k++;
+                load_interval<XS_ARITH_FAST>(t, nuc, k, v);
+            }
+        }
+        if (GRID == XS_HASH && v[11] == E) {
+            // E on a gridpoint: the reference's own hash search and edge rule
+            load_interval<XS_ARITH_FAST>(t, nuc, interval_hash<CHECKED>(t, bin, nuc, q, err), v);
+        }
+        accumulate_loaded<XS_ARITH_FAST, DE>(v, E, conc, macro, S);
+    }
+    return true;
+}
+
 // ------------------------------------------------------------ one lookup ---
 // calculate_macro_xs (Simulation.c:326-375) for one (E, mat).
 // With DE, S[5] receives d macro_xs / dE (the adjoint's energy derivative).
@@ -661,6 +876,12 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
                                                             S, q0, stride);
         return;
     }
+    if (ARITH == XS_ARITH_FAST && t.binrec &&
+        macro_xs_binned<GRID, CHECKED, DE, SROW>(t, E, n, mrow, crow, macro, err, S, q0, stride))
+        return;
+    if (t.guide && macro_xs_guided<GRID, ARITH, CHECKED, DE, SROW>(t, E, n, mrow, crow, macro, err,
+                                                                    S, q0, stride))
+        return;
     long row = 0;
     long long q = 0;
     const bool keyed = !(E != E);   // NaN energies use the double-compare path

@@ -231,13 +231,28 @@ PlainScratch carve_plain_scratch(void *buf, long count, int tile)
     return p;
 }
 
-xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                       long count, int tile, const SampleInput &in, const Outputs &out,
-                       const PlainScratch *ps, int *launches)
+int list_blocks(const xs_ctx *ctx, int block)
 {
-    if (tile < kBlock || tile % kBlock) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d must be a multiple of %d", tile, kBlock);
+    if (block <= 0) block = ctx->batched_block;
+    const int b = ctx->sm_count * ctx->batched_blocks_per_sm * kBlock / block;
+    return b > 0 ? b : 1;
+}
+
+xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
+                       long count, int tile, int block, const SampleInput &in,
+                       const Outputs &out, const PlainScratch *ps, int *launches)
+{
+    if (block == 0) {
+        block = ctx->plain_block;
+        while (block > tile && block > 128) block >>= 1;
+    }
+    if (block != 128 && block != 256 && block != 512)
+        return fail(XS_ERR_INVALID_ARGUMENT, "block_threads %d: 128, 256 or 512", block);
+    if (tile < block || tile % block)
+        return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d must be a multiple of the block size %d", tile, block);
     if (tile > 8192) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d above 8192", tile);
     PlainArgs a;
+    a.block = block;
     a.first = first;
     a.count = count;
     a.tile = tile;
@@ -277,8 +292,8 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
         l.fuel_lanes = ctx->fuel_lanes;  // the plain kernel's arithmetic, lookup for lookup
         l.table = 0;
         l.sorted = 0;
-        XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
-                                          ctx->sm_count * ctx->batched_blocks_per_sm, l));
+        l.block = ctx->batched_block;
+        XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, list_blocks(ctx, l.block), l));
         if (launches) *launches += 2;
     }
     return XS_OK;
@@ -308,9 +323,10 @@ BatchedScratch carve_batched_scratch(void *buf, long count, int nb_log2)
 // The batched run on explicit buffers (b.verification / b.error set): clears
 // the bucket offsets and the queue, sorts, runs the lookups.  Four launches.
 xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                              long count, int nb_log2, const SampleInput &in, const Outputs &out,
-                              const BatchedScratch &b, int *launches)
+                              long count, int nb_log2, int block, const SampleInput &in,
+                              const Outputs &out, const BatchedScratch &b, int *launches)
 {
+    if (block <= 0) block = ctx->batched_block;
     const int nb = 1 << nb_log2;
     XS_CUDA(cudaMemsetAsync(b.offs, 0, (size_t)kMaterials * nb * 4, st));
     XS_CUDA(cudaMemsetAsync(b.queue, 0, sizeof(unsigned int), st));
@@ -348,21 +364,22 @@ xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int check
     l.fuel_lanes = ctx->batched_fuel_lanes;
     l.table = 1;
     l.sorted = 1;
-    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked,
-                                      ctx->sm_count * ctx->batched_blocks_per_sm, l));
+    l.block = block;
+    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, list_blocks(ctx, block), l));
     if (launches) *launches += 4;
     return XS_OK;
 }
 
 static xs_status enqueue_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                                 long count, int nb_log2, const SampleInput &in,
+                                 long count, int nb_log2, int block, const SampleInput &in,
                                  const Outputs &out, int *launches)
 {
     BatchedScratch b = carve_batched_scratch(ctx->s.sort_buf, count, nb_log2);
     b.queue = ctx->s.queue;
     b.verification = ctx->s.verification;
     b.error = ctx->s.error;
-    return enqueue_batched_buf(ctx, st, arith, checked, first, count, nb_log2, in, out, b, launches);
+    return enqueue_batched_buf(ctx, st, arith, checked, first, count, nb_log2, block, in, out, b,
+                               launches);
 }
 
 // The (material, energy-bucket) counting sort alone, for the adjoint: fills
@@ -439,8 +456,8 @@ xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first
     l.fuel_lanes = ctx->batched_fuel_lanes;
     l.table = 1;
     l.sorted = 1;
-    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, 0,
-                                      ctx->sm_count * ctx->batched_blocks_per_sm, l));
+    l.block = ctx->batched_block;
+    XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, 0, list_blocks(ctx, l.block), l));
     return XS_OK;
 }
 
@@ -448,7 +465,9 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
                          long count, int block, int buckets, const SampleInput &in,
                          const Outputs &out, int *launches)
 {
-    (void)block;
+    if (block <= 0) block = ctx->batched_block;
+    if (block != 128 && block != 256 && block != 512)
+        return fail(XS_ERR_INVALID_ARGUMENT, "block_threads %d: 128, 256 or 512", block);
     if (buckets < 1 || (buckets & (buckets - 1)) || buckets > 65536)
         return fail(XS_ERR_INVALID_ARGUMENT, "energy_buckets %d must be a power of two <= 65536", buckets);
     if (count > 0x7FFFFFFFL - kMaterials * 32)
@@ -474,9 +493,9 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
     }
     char key[256];
     // everything the captured launches bake in: options, pointers, grid view
-    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d/%d/%p/%p/%d/%d", arith, checked,
+    snprintf(key, sizeof key, "%d/%d/%ld/%ld/%d/%p/%p/%p/%p/%p/%d/%d/%d/%p/%p/%d/%d", arith, checked,
              first, count, nb_log2, (const void *)in.energy, (const void *)in.mat,
-             (void *)out.macro, (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm,
+             (void *)out.macro, (void *)out.max_idx, (void *)st, ctx->batched_blocks_per_sm, block,
              ctx->t.grid_type, (const void *)ctx->t.index_grid, (const void *)ctx->t.coarse,
              ctx->t.hash_bins, ctx->batched_fuel_lanes * 2 + (ctx->t.utab[0] != nullptr));
     auto it = ctx->graphs.find(key);
@@ -490,7 +509,8 @@ xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, l
             return cuda_fail(e, "cudaStreamBeginCapture");
         }
         int n = 0;
-        xs_status s = enqueue_batched(ctx, cap, arith, checked, first, count, nb_log2, in, out, &n);
+        xs_status s = enqueue_batched(ctx, cap, arith, checked, first, count, nb_log2, block, in, out,
+                                      &n);
         e = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
         if (s != XS_OK) {
@@ -592,7 +612,7 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
     Outputs out;
     out.macro = macro;
     for (int step = 0; step < nl; step++) {
-        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, in, out, nullptr, &n);
+        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, 0, in, out, nullptr, &n);
         if (s != XS_OK) return s;
         if (step + 1 < nl) {
             k_history_advance<<<blocks, 256, 0, st>>>(ctx->t, count, macro, seed, E, mat);

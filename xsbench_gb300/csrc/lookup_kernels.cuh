@@ -7,7 +7,8 @@
 
 namespace xsgb {
 
-constexpr int kBlock = 256;          // threads per block of every lookup kernel
+constexpr int kBlock = 256;          // threads per block of the lookup kernels (the plain and
+                                     // list kernels also come in 128 and 512; the tuner picks)
 constexpr int kWarps = kBlock / 32;
 #ifndef XSGB_PLAIN_MIN_BLOCKS
 #define XSGB_PLAIN_MIN_BLOCKS 4      // resident blocks per SM the compiler must allow
@@ -39,6 +40,7 @@ struct PlainArgs {
     // (rows_total entries in all) in shared memory
     int stage_rows;
     int rows_total;
+    int block;                   // threads per block: 128, 256 or 512 (tile a multiple of it)
 };
 
 // A material-segmented list of lookups (the batched sort, or the plain
@@ -60,6 +62,7 @@ struct ListArgs {
     int fuel_lanes;              // lanes per fuel lookup (PlainArgs::fuel_lanes)
     int table;                   // 1: read the union table when there is one (FAST)
     int sorted;                  // 1: entries sorted by energy bucket (warp searches pay)
+    int block;                   // threads per block of the persistent kernel: 128, 256 or 512
 };
 
 // Adds the per-lane verification counts of a block into *verif (one atomic).
@@ -196,8 +199,8 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
 // different row of a table of ~155 GB, and the page-translation misses of that
 // pattern cost more than the bytes it saves (the batched kernel, whose warps
 // read neighbouring rows, uses it).
-template <int GRID, int ARITH, bool CHECKED, bool SAMPLES, bool SROW = false>
-__global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables t, PlainArgs a)
+template <int GRID, int ARITH, bool CHECKED, bool SAMPLES, bool SROW = false, int BLOCK = kBlock>
+__global__ void __launch_bounds__(BLOCK, XSGB_PLAIN_MIN_BLOCKS * kBlock / BLOCK) k_plain(Tables t, PlainArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tile = a.tile;
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
         __syncthreads();
         for (int m = 0; m < kMaterials; m++) {
             const int o0 = roff[m], n = roff[m + 1] - o0;
-            for (int j = threadIdx.x; j < n; j += kBlock) {
+            for (int j = threadIdx.x; j < n; j += BLOCK) {
                 sc[o0 + j] = ldg(&t.concs[m * t.max_nucs + j]);
                 sm[o0 + j] = ldg(&t.mats[m * t.max_nucs + j]);
             }
@@ -247,9 +250,9 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
 
     // sample: LCG threads take consecutive lookups (one skip-ahead each);
     // caller samples are read with a coalesced stride.
-    const int lpt = tile / kBlock;
+    const int lpt = tile / BLOCK;
     if (SAMPLES) {
-        for (int l = tid; l < ntile; l += kBlock) {
+        for (int l = tid; l < ntile; l += BLOCK) {
             unsigned long long seed = 0;
             double E;
             int m;
@@ -289,14 +292,14 @@ __global__ void __launch_bounds__(kBlock, XSGB_PLAIN_MIN_BLOCKS) k_plain(Tables 
         obase[tid] = rem ? atomicAdd(&a.ovf_cnt[tid], rem) : 0;
     }
     __syncthreads();
-    for (int l = tid; l < ntile; l += kBlock) {
+    for (int l = tid; l < ntile; l += BLOCK) {
         int m = sMat[l];
         if (m != 0xFF) perm[atomicAdd(&cur[m], 1)] = l;
     }
     __syncthreads();
     if (overflow) {
         // remainders: positions [seg+full, seg+cnt) of each material
-        for (int r = tid; r < kMaterials * 32; r += kBlock) {
+        for (int r = tid; r < kMaterials * 32; r += BLOCK) {
             const int m = r >> 5, q = r & 31;
             const int full = cnt[m] & ~31;
             if (q < (cnt[m] & 31)) {
@@ -422,15 +425,15 @@ __device__ __forceinline__ void list_lookup_body(const Tables &t, const ListArgs
     block_verification(mine, &s_acc, a.verif);
 }
 
-template <int GRID, int ARITH, bool CHECKED>
-__global__ void __launch_bounds__(kBlock) k_list_lookup(Tables t, ListArgs a)
+template <int GRID, int ARITH, bool CHECKED, int BLOCK = kBlock>
+__global__ void __launch_bounds__(BLOCK) k_list_lookup(Tables t, ListArgs a)
 {
     list_lookup_body<GRID, ARITH, CHECKED, false>(t, a);
 }
 
 // The union-table variant (FAST): more registers for loads in flight.
-template <int GRID>
-__global__ void __launch_bounds__(kBlock, 2) k_list_lookup_table(Tables t, ListArgs a)
+template <int GRID, int BLOCK = kBlock>
+__global__ void __launch_bounds__(BLOCK, 2 * kBlock / BLOCK) k_list_lookup_table(Tables t, ListArgs a)
 {
     list_lookup_body<GRID, XS_ARITH_FAST, false, true>(t, a);
 }
@@ -548,19 +551,30 @@ struct GridLaunch {
         const size_t sm = plain_smem_bytes(a.tile, srow ? a.rows_total : 0);
         // shared-memory share of the SM's 228 KB that holds the resident
         // blocks (each with its static arrays and 1 KB reserved), L1 the rest
-        const int carve = srow ? (int)((XSGB_PLAIN_MIN_BLOCKS * (sm + 1280) * 100 + 233471) / 233472)
-                               : 25;
-#define XSGB_PLAIN_R(A, C, S, R)                                                              \
+        // (the resident blocks: XSGB_PLAIN_MIN_BLOCKS of 256 threads, or as
+        // many threads in blocks of a.block)
+        const int blk = (!checked && (a.block == 128 || a.block == 512)) ? a.block : kBlock;
+        const size_t resident = (size_t)XSGB_PLAIN_MIN_BLOCKS * kBlock / blk;
+        const int need = (int)((resident * (sm + 1280) * 100 + 233471) / 233472);
+        const int carve = srow ? need : (need > 25 ? need : 25);
+#define XSGB_PLAIN_RB(A, C, S, R, B)                                                          \
     do {                                                                                      \
-        auto k = k_plain<GRID, A, C, S, R>;                                                   \
+        auto k = k_plain<GRID, A, C, S, R, B>;                                                \
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                              (int)sm);                                        \
         if (e == cudaSuccess)                                                                 \
             e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,       \
                                      carve < 100 ? carve : 100);                              \
         if (e != cudaSuccess) return e;                                                       \
-        k<<<(unsigned)blocks, kBlock, sm, st>>>(t, a);                                        \
+        k<<<(unsigned)blocks, B, sm, st>>>(t, a);                                             \
         return cudaGetLastError();                                                            \
+    } while (0)
+        // unchecked variants in three block sizes; checked runs use 256
+#define XSGB_PLAIN_R(A, C, S, R)                                       \
+    do {                                                               \
+        if (!(C) && a.block == 128) XSGB_PLAIN_RB(A, C, S, R, 128);    \
+        if (!(C) && a.block == 512) XSGB_PLAIN_RB(A, C, S, R, 512);    \
+        XSGB_PLAIN_RB(A, C, S, R, kBlock);                             \
     } while (0)
 #define XSGB_PLAIN(A, C, S) XSGB_PLAIN_R(A, C, S, false)
         if (srow) {
@@ -579,26 +593,40 @@ struct GridLaunch {
         XSGB_PLAIN(XS_ARITH_FAST, false, false);
 #undef XSGB_PLAIN
 #undef XSGB_PLAIN_R
+#undef XSGB_PLAIN_RB
     }
 
     static cudaError_t list(const Tables &t, cudaStream_t st, int arith, int checked, int blocks,
                             const ListArgs &a)
     {
-#define XSGB_LIST(A, C)                                                      \
+        // `blocks` persistent blocks of a.block threads (checked runs: 256)
+#define XSGB_LIST_B(A, C, B)                                                 \
     do {                                                                     \
-        k_list_lookup<GRID, A, C><<<blocks, kBlock, 0, st>>>(t, a);          \
+        k_list_lookup<GRID, A, C, B><<<blocks, B, 0, st>>>(t, a);            \
         return cudaGetLastError();                                           \
+    } while (0)
+#define XSGB_LIST(A, C)                                     \
+    do {                                                    \
+        if (!(C) && a.block == 128) XSGB_LIST_B(A, C, 128); \
+        if (!(C) && a.block == 512) XSGB_LIST_B(A, C, 512); \
+        XSGB_LIST_B(A, C, kBlock);                          \
     } while (0)
         if (checked) XSGB_LIST(XS_ARITH_FAST, true);
         if (arith == XS_ARITH_EXACT) XSGB_LIST(XS_ARITH_EXACT, false);
         if constexpr (GRID == XS_UNIONIZED) {
             if (a.table && t.utab[0] != nullptr) {
-                k_list_lookup_table<GRID><<<blocks, kBlock, 0, st>>>(t, a);
+                if (a.block == 128)
+                    k_list_lookup_table<GRID, 128><<<blocks, 128, 0, st>>>(t, a);
+                else if (a.block == 512)
+                    k_list_lookup_table<GRID, 512><<<blocks, 512, 0, st>>>(t, a);
+                else
+                    k_list_lookup_table<GRID><<<blocks, kBlock, 0, st>>>(t, a);
                 return cudaGetLastError();
             }
         }
         XSGB_LIST(XS_ARITH_FAST, false);
 #undef XSGB_LIST
+#undef XSGB_LIST_B
     }
 
     static cudaError_t adjoint(const Tables &t, cudaStream_t st, int blocks, const ListArgs &a,

@@ -23,9 +23,6 @@
 
 namespace xsgb {
 
-__global__ void k_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, double du,
-                            int *index);
-
 constexpr int kGenPerThread = 64;
 
 __global__ void k_gen_points(long n_pts, xs_gridpoint *g)
@@ -331,7 +328,8 @@ extern "C" xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs
             void *idx = nullptr;
             s = ctx_alloc(ctx, &idx, (size_t)in->hash_bins * n_iso * 4);
             if (s != XS_OK) break;
-            k_hash_grid<<<sm * 8, 256, 0, st>>>(t.grid, n_iso, n_gp, in->hash_bins, 1.0 / in->hash_bins, (int *)idx);
+            if ((e = launch_hash_grid(t.grid, n_iso, n_gp, in->hash_bins, (int *)idx, sm, st)) != cudaSuccess)
+                break;
             t.index_grid = (const int *)idx;
         }
         if ((e = cudaGetLastError()) != cudaSuccess) break;

@@ -12,7 +12,12 @@
 // The array is a file-scope __device__ variable, so every GPU that loads the
 // library holds it (6.5 MB) until the process exits.  Its name is only a
 // host-side stand-in in host code; the device address comes from
-// cudaGetSymbolAddress, looked up once per device on that device's first call.
+// cudaGetSymbolAddress, looked up with the device current on the first call
+// on each device, and again on the first call after that device's CUDA
+// context was re-created (a cudaDeviceReset elsewhere in the process), when
+// the array may sit at another address.
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
 
@@ -32,23 +37,64 @@ constexpr size_t kStaticBytes =
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 static std::mutex g_static_mu;
-static void *g_static_addr[64];  // device address per device ordinal
+// per device ordinal: the array's device address and the id of the CUDA
+// context it was looked up in
+struct StaticAddr {
+    unsigned long long ctx_id;
+    void *addr;
+};
+static StaticAddr g_static_addr[64];
 
+typedef CUresult (*PFN_ctx_current)(CUcontext *);
+typedef CUresult (*PFN_ctx_id)(CUcontext, unsigned long long *);
+
+// Unique id of the calling thread's current CUDA context (ids are never
+// reused within a process, unlike context handles); 0 when unavailable.
+static unsigned long long current_context_id()
+{
+    static PFN_ctx_current get_current = nullptr;
+    static PFN_ctx_id get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = (PFN_ctx_current)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_ctx_id)f;
+        cudaGetLastError();
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of g_static_scratch on `device`, which must be current.
 static xs_status static_scratch_address(int device, unsigned char **out)
 {
     if (device < 0 || device >= 64) return fail(XS_ERR_NO_DEVICE, "device ordinal %d", device);
+    const unsigned long long id = current_context_id();
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_addr[device]) {
+    StaticAddr &e = g_static_addr[device];
+    if (!e.addr || id == 0 || e.ctx_id != id) {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_scratch)");
-        g_static_addr[device] = p;
+        cudaError_t err = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(g_static_scratch)");
+        e.addr = p;
+        e.ctx_id = id;
     }
-    *out = (unsigned char *)g_static_addr[device];
+    *out = (unsigned char *)e.addr;
     return XS_OK;
 }
 
-static bool device_or_null(const void *p)
+// NULL, or memory the kernels on `device` can write: device memory of that
+// device, or managed memory.
+static bool device_or_null(const void *p, int device)
 {
     if (!p) return true;
     cudaPointerAttributes a;
@@ -56,8 +102,28 @@ static bool device_or_null(const void *p)
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == device;
 }
+
+// Makes `device` current for the scope and puts the caller's device back.
+struct DeviceScope {
+    int saved = -1;
+    cudaError_t set(int device)
+    {
+        cudaError_t e = cudaGetDevice(&saved);
+        if (e != cudaSuccess) {
+            saved = -1;
+            return e;
+        }
+        return saved == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceScope()
+    {
+        int now = -1;
+        if (saved >= 0 && cudaGetDevice(&now) == cudaSuccess && now != saved) cudaSetDevice(saved);
+    }
+};
 
 }  // namespace xsgb
 
@@ -75,16 +141,21 @@ extern "C" xs_status xs_run_event_batched_static(xs_ctx *ctx, long first, long c
         return fail(XS_ERR_INVALID_ARGUMENT,
                     "xs_run_event_batched_static: %ld lookups exceed the static scratch (at most %ld per call)",
                     count, kStaticMaxLookups);
-    if (energy_buckets <= 0) energy_buckets = 1024;
+    // default: the context's batched bucket count (tuned), within the array's limit
+    if (energy_buckets <= 0)
+        energy_buckets = ctx->batched_buckets < kStaticMaxBuckets ? ctx->batched_buckets : kStaticMaxBuckets;
     if (energy_buckets > kStaticMaxBuckets || (energy_buckets & (energy_buckets - 1)))
         return fail(XS_ERR_INVALID_ARGUMENT,
                     "xs_run_event_batched_static: energy_buckets %d must be a power of two <= %d",
                     energy_buckets, kStaticMaxBuckets);
     if (arith != XS_ARITH_FAST && arith != XS_ARITH_EXACT)
         return fail(XS_ERR_INVALID_ARGUMENT, "xs_run_event_batched_static: unknown arithmetic %d", arith);
-    XS_CUDA(cudaSetDevice(ctx->device));
-    if (!device_or_null(macro_xs_out) || !device_or_null(max_idx_out))
-        return fail(XS_ERR_INVALID_ARGUMENT, "xs_run_event_batched_static: outputs must be device memory or NULL");
+    DeviceScope scope;   // the caller's current device is restored on return
+    XS_CUDA(scope.set(ctx->device));
+    if (!device_or_null(macro_xs_out, ctx->device) || !device_or_null(max_idx_out, ctx->device))
+        return fail(XS_ERR_INVALID_ARGUMENT,
+                    "xs_run_event_batched_static: outputs must be NULL or device memory of the context's device %d",
+                    ctx->device);
     unsigned char *base = nullptr;
     xs_status s = static_scratch_address(ctx->device, &base);
     if (s != XS_OK) return s;

@@ -59,6 +59,87 @@ __global__ void k_coarse(const long long *ekeys, long n_iso, long n_gp, int n_co
     }
 }
 
+// Hash grid of GridInit.c:128-151: index[e][nuc] = grid_search_nuclide of the
+// bin edge e * du over the nuclide's whole grid (Simulation.c:403-423).
+__global__ void k_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, double du,
+                            int *index)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (long)bins * n_iso;
+         i += (long)gridDim.x * blockDim.x) {
+        const long e = i / n_iso, nuc = i - e * n_iso;
+        const double energy = e * du;
+        const xs_gridpoint *A = grid + nuc * n_gp;
+        long lo = 0, hi = n_gp - 1;
+        while (hi - lo > 1) {
+            long mid = lo + (hi - lo) / 2;
+            if (A[mid].energy > energy) hi = mid; else lo = mid;
+        }
+        index[i] = (int)lo;
+    }
+}
+
+// Energy-bin guide of each nuclide: for 2^k bins over [0, 1),
+// guide[nuc][b] = #{j : E_j < b / 2^k}.  Thread (nuc, j) for j = 0 .. n_gp
+// writes j into the bins b with E_{j-1} < b / 2^k <= E_j (E_{-1} = -inf,
+// E_{n_gp} = +inf): on a sorted grid these ranges partition 0 .. 2^k, so
+// every entry is written exactly once.  b / 2^k <= E  <=>  b <= floor(E 2^k),
+// exact in integers for E in [0, 1).
+__device__ __forceinline__ long guide_floor(double E, int k)
+{
+    if (!(E >= 0.0)) return -1;                 // negative (or NaN: ordered last by the sort)
+    if (E >= 1.0) return 1L << k;
+    return xsgb_floor_scaled_pow2(E, k);
+}
+
+__global__ void k_guide(const xs_gridpoint *grid, long n_iso, long n_gp, int k, int *guide)
+{
+    const long nb = (1L << k) + 1;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n_iso * (n_gp + 1);
+         i += (long)gridDim.x * blockDim.x) {
+        const long nuc = i / (n_gp + 1), j = i - nuc * (n_gp + 1);
+        const xs_gridpoint *A = grid + nuc * n_gp;
+        long lo = j == 0 ? 0 : guide_floor(A[j - 1].energy, k) + 1;
+        long hi = j == n_gp ? nb - 1 : guide_floor(A[j].energy, k);
+        if (lo < 0) lo = 0;
+        if (hi > nb - 1) hi = nb - 1;
+        int *g = guide + nuc * nb;
+        for (long b = lo; b <= hi; b++) g[b] = (int)j;
+    }
+}
+
+// Bin records: slot (nuc, b) = the record of interval
+// clamp(guide[nuc][b] - 1, 0, n_gp - 2).
+__global__ void k_bin_records(const double2 *rec, const int *guide, long n_iso, long n_gp, int k,
+                              double2 *out)
+{
+    const long nb = 1L << k;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n_iso * nb;
+         i += (long)gridDim.x * blockDim.x) {
+        const long nuc = i >> k, b = i & (nb - 1);
+        long k0 = (long)guide[nuc * (nb + 1) + b] - 1;
+        if (k0 < 0) k0 = 0;
+        if (k0 > n_gp - 2) k0 = n_gp - 2;
+        const double2 *src = rec + (nuc * (n_gp - 1) + k0) * kRecordPairs;
+        double2 *dst = out + i * kRecordPairs;
+#pragma unroll
+        for (int q = 0; q < kRecordPairs; q++) dst[q] = src[q];
+    }
+}
+
+cudaError_t launch_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, int *index,
+                             int sm_count, cudaStream_t st)
+{
+    k_hash_grid<<<sm_count * 8, 256, 0, st>>>(grid, n_iso, n_gp, bins, 1.0 / bins, index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_keys(const long long *ekeys, long n_iso, long n_gp, int n_coarse,
+                               long long *coarse, int sm_count, cudaStream_t st)
+{
+    k_coarse<<<sm_count * 8, 256, 0, st>>>(ekeys, n_iso, n_gp, n_coarse, coarse);
+    return cudaGetLastError();
+}
+
 __global__ void k_double_keys(const double *v, long n, long long *keys)
 {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -156,6 +237,68 @@ xs_status build_union_table(xs_ctx *ctx)
     return XS_OK;
 }
 
+// The energy-bin guide (Tables::guide) and the bin records
+// (Tables::binrec): about four bins per gridpoint (2^(ceil(log2 n_gp) + 2),
+// at most 2^26 per nuclide), so most bins hold no gridpoint and a lookup's
+// interval is the bin's first one.  Built for the hash and nuclide grids (and
+// by the autotuner when it serves a unionized context from those);
+// XSGB_GUIDE=0 in the environment leaves both out, and so does a device
+// without room for them (the searches then run without them).
+xs_status build_guide(xs_ctx *ctx)
+{
+    Tables &t = ctx->t;
+    t.guide = nullptr;
+    t.guide_log2 = 0;
+    t.binrec = nullptr;
+    if (const char *env = getenv("XSGB_GUIDE"))
+        if (atoi(env) == 0) return XS_OK;
+    int k = 2;
+    while (k < 26 && (1L << (k - 2)) < t.n_gp) k++;
+    if (const char *env = getenv("XSGB_GUIDE_LOG2")) {
+        const int v = atoi(env);
+        if (v >= 1 && v <= 26) k = v;
+    }
+    const size_t bytes = (size_t)t.n_iso * (((size_t)1 << k) + 1) * 4;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return XS_OK;
+    }
+    if (free_b < bytes + ((size_t)4 << 30)) return XS_OK;
+    void *p = nullptr;
+    xs_status s = ctx_alloc(ctx, &p, bytes);
+    if (s != XS_OK) return s;
+    k_guide<<<grid_for((long)t.n_iso * (t.n_gp + 1), ctx->sm_count), 256, 0, ctx->stream>>>(
+        t.grid, t.n_iso, t.n_gp, k, (int *)p);
+    XS_CUDA(cudaGetLastError());
+    t.guide = (const int *)p;
+    t.guide_log2 = k;
+
+    // bin records: 128 bytes per (nuclide, bin), when the device keeps 16 GiB
+    // beside them; XSGB_BIN_RECORDS=0 leaves them out
+    t.binrec = nullptr;
+    t.bin_prefetch = 1;
+    if (const char *env = getenv("XSGB_BIN_PREFETCH")) {
+        const int v = atoi(env);
+        if (v >= 0 && v <= 4) t.bin_prefetch = v;
+    }
+    if (const char *env = getenv("XSGB_BIN_RECORDS"))
+        if (atoi(env) == 0) return XS_OK;
+    const size_t rbytes = (size_t)t.n_iso * ((size_t)1 << k) * kRecordDoubles * 8;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return XS_OK;
+    }
+    if (free_b < rbytes + ((size_t)16 << 30)) return XS_OK;
+    s = ctx_alloc(ctx, &p, rbytes);
+    if (s != XS_OK) return s;
+    k_bin_records<<<grid_for((long)t.n_iso << k, ctx->sm_count), 256, 0, ctx->stream>>>(
+        t.records, t.guide, t.n_iso, t.n_gp, k, (double2 *)p);
+    XS_CUDA(cudaGetLastError());
+    t.binrec = (const double2 *)p;
+    return XS_OK;
+}
+
 xs_status build_derived_tables(xs_ctx *ctx)
 {
     Tables &t = ctx->t;
@@ -195,6 +338,10 @@ xs_status build_derived_tables(xs_ctx *ctx)
         t.coarse = (const long long *)p;
         k_coarse<<<grid_for((long)t.n_iso * t.n_coarse, sm), 256, 0, st>>>(t.ekeys, t.n_iso, t.n_gp, t.n_coarse, (long long *)p);
         XS_CUDA(cudaGetLastError());
+    }
+    if (t.grid_type != XS_UNIONIZED) {   // the searches of the hash and nuclide grids
+        s = build_guide(ctx);
+        if (s != XS_OK) return s;
     }
     if (t.grid_type == XS_UNIONIZED) {
         s = ctx_alloc(ctx, &p, (size_t)t.n_union * 8);

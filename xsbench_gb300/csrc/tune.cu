@@ -19,33 +19,6 @@
 
 namespace xsgb {
 
-__global__ void k_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, double du,
-                            int *index)
-{
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (long)bins * n_iso;
-         i += (long)gridDim.x * blockDim.x) {
-        const long e = i / n_iso, nuc = i - e * n_iso;
-        const double energy = e * du;
-        const xs_gridpoint *A = grid + nuc * n_gp;
-        long lo = 0, hi = n_gp - 1;  // Simulation.c:403-423
-        while (hi - lo > 1) {
-            long mid = lo + (hi - lo) / 2;
-            if (A[mid].energy > energy) hi = mid; else lo = mid;
-        }
-        index[i] = (int)lo;
-    }
-}
-
-__global__ void k_coarse_keys(const long long *ekeys, long n_iso, long n_gp, int n_coarse,
-                              long long *coarse)
-{
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n_iso * n_coarse;
-         i += (long)gridDim.x * blockDim.x) {
-        const long nuc = i / n_coarse, c = i - nuc * n_coarse;
-        coarse[i] = ekeys[nuc * n_gp + c * kCoarseStride];
-    }
-}
-
 // The fields of Tables that differ between grid types.
 struct GridView {
     int grid_type, hash_bins;
@@ -86,6 +59,7 @@ static std::string cache_key(const xs_ctx *ctx)
 struct Choice {
     int grid_type = -1, kernel = 0, tile = 1024, buckets = 4096, blocks_per_sm = 4, lanes = 1;
     double rate = 0;
+    int block = 256;   // threads per block of the chosen kernel
 };
 
 // cache file: one entry per line, {"<key>": {...}} inside a JSON object
@@ -101,10 +75,12 @@ static bool cache_read(const char *path, const std::string &key, Choice &c)
         if (!p) continue;
         p += want.size();
         if (sscanf(p, " {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
-                      "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"lookups_per_s\": %lf",
+                      "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"block\": %d, "
+                      "\"lookups_per_s\": %lf",
                    &c.grid_type, &c.kernel, &c.tile, &c.buckets, &c.blocks_per_sm, &c.lanes,
-                   &c.rate) == 7 &&
-            (c.lanes == 1 || c.lanes == 2 || c.lanes == 4))
+                   &c.block, &c.rate) == 8 &&
+            (c.lanes == 1 || c.lanes == 2 || c.lanes == 4) &&
+            (c.block == 128 || c.block == 256 || c.block == 512) && c.tile % c.block == 0)
             found = true;
     }
     fclose(f);
@@ -129,9 +105,9 @@ static void cache_write(const char *path, const std::string &key, const Choice &
     char buf[1024];
     snprintf(buf, sizeof buf,
              "  \"%s\": {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
-             "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"lookups_per_s\": %.6g}",
+             "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"block\": %d, \"lookups_per_s\": %.6g}",
              key.c_str(), c.grid_type, c.kernel, c.tile, c.buckets, c.blocks_per_sm, c.lanes,
-             c.rate);
+             c.block, c.rate);
     lines.push_back(buf);
     FILE *f = fopen(path, "w");
     if (!f) return;
@@ -162,8 +138,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         const int bins = 10000;
         xs_status s = ctx_alloc(ctx, &p, (size_t)bins * t.n_iso * 4);
         if (s != XS_OK) return s;
-        k_hash_grid<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(t.grid, t.n_iso, t.n_gp, bins, 1.0 / bins, (int *)p);
-        XS_CUDA(cudaGetLastError());
+        XS_CUDA(launch_hash_grid(t.grid, t.n_iso, t.n_gp, bins, (int *)p, ctx->sm_count, ctx->stream));
         ctx->tune_hash_index = (int *)p;
     }
     if (!base.coarse && !ctx->tune_coarse) {
@@ -171,10 +146,14 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         const int nc = (int)((t.n_gp + kCoarseStride - 1) / kCoarseStride);
         xs_status s = ctx_alloc(ctx, &p, (size_t)t.n_iso * nc * 8);
         if (s != XS_OK) return s;
-        k_coarse_keys<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(t.ekeys, t.n_iso, t.n_gp, nc, (long long *)p);
-        XS_CUDA(cudaGetLastError());
+        XS_CUDA(launch_coarse_keys(t.ekeys, t.n_iso, t.n_gp, nc, (long long *)p, ctx->sm_count,
+                                   ctx->stream));
         ctx->tune_coarse = (long long *)p;
         ctx->tune_n_coarse = nc;
+    }
+    if (!t.guide) {   // the guided searches of the hash and nuclide grids
+        xs_status s = build_guide(ctx);
+        if (s != XS_OK) return s;
     }
     if (base.grid_type != XS_HASH)
         views.push_back(GridView{XS_HASH, 10000, 1.0 / 10000, ctx->tune_hash_index, base.coarse,
@@ -206,12 +185,17 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         };
         const int saved_bps = ctx->batched_blocks_per_sm;
         const int saved_lanes = ctx->fuel_lanes, saved_blanes = ctx->batched_fuel_lanes;
+        const int saved_pblock = ctx->plain_block, saved_bblock = ctx->batched_block;
         auto restore = [&]() {
             apply_view(t, original);
             ctx->batched_blocks_per_sm = saved_bps;
             ctx->fuel_lanes = saved_lanes;
             ctx->batched_fuel_lanes = saved_blanes;
+            ctx->plain_block = saved_pblock;
+            ctx->batched_block = saved_bblock;
         };
+        // the shapes are searched at 256 threads per block, the block size after
+        ctx->plain_block = ctx->batched_block = 256;
         for (const GridView &v : views) {
             apply_view(t, v);
             for (int bps : {3, 4}) {
@@ -230,7 +214,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                             restore();
                             return s;
                         }
-                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, lanes, rate};
+                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, lanes, rate, 256};
                     }
                     for (int nb : {256, 1024, 4096, 16384}) {
                         xs_run_opts o;
@@ -244,9 +228,37 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                             restore();
                             return s;
                         }
-                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, lanes, rate};
+                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, lanes, rate, 256};
                     }
                 }
+            }
+        }
+        // block shape of the chosen kernel, with the rest of the choice in
+        // place and the threads per SM unchanged (the plain kernel's blocks
+        // divide its tile)
+        for (const GridView &v : views)
+            if (v.grid_type == c.grid_type) apply_view(t, v);
+        ctx->batched_blocks_per_sm = c.blocks_per_sm;
+        ctx->fuel_lanes = c.lanes;
+        ctx->batched_fuel_lanes = c.lanes;
+        for (int block : {128, 512}) {
+            if (c.kernel == XS_KERNEL_PLAIN && c.tile % block) continue;
+            xs_run_opts o;
+            xs_run_opts_init(&o);
+            o.count = sample;
+            o.kernel = c.kernel;
+            o.tile_lookups = c.tile;
+            o.energy_buckets = c.buckets;
+            o.block_threads = block;
+            double rate = 0;
+            xs_status s = time_run(o, &rate);
+            if (s != XS_OK) {
+                restore();
+                return s;
+            }
+            if (rate > c.rate) {
+                c.rate = rate;
+                c.block = block;
             }
         }
         restore();
@@ -258,10 +270,13 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
     ctx->plain_tile = c.tile;
     ctx->batched_buckets = c.buckets;
     ctx->batched_blocks_per_sm = c.blocks_per_sm;
-    if (c.kernel == XS_KERNEL_PLAIN)
+    if (c.kernel == XS_KERNEL_PLAIN) {
         ctx->fuel_lanes = c.lanes;
-    else
+        ctx->plain_block = c.block;
+    } else {
         ctx->batched_fuel_lanes = c.lanes;
+        ctx->batched_block = c.block;
+    }
     for (auto &kv : ctx->graphs) cudaGraphExecDestroy(kv.second.exec);
     ctx->graphs.clear();
     if (best) {
@@ -269,6 +284,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         best->kernel = c.kernel;
         best->tile_lookups = c.tile;
         best->energy_buckets = c.buckets;
+        best->block_threads = c.block;
     }
     return XS_OK;
 }

@@ -48,6 +48,17 @@ struct Tables {
     const long long *union_keys;     // [n_union]
     const int *union_bins;           // [2^b + 1]
     const int *index_grid;           // UEG: [n_union * n_iso]  HASH: [hash_bins * n_iso]
+    // energy-bin guide of each nuclide (searches of the hash and nuclide
+    // grids): guide[nuc * (2^guide_log2 + 1) + b] = #{j : E_j < b * 2^-guide_log2},
+    // b = 0 .. 2^guide_log2; null when not built
+    const int *guide;
+    int guide_log2;
+    // bin records (FAST): for nuclide nuc and guide bin b, a copy of the
+    // interval record of interval clamp(guide[nuc][b] - 1, 0, n_gp - 2) -- the
+    // interval holding the bin's lower edge -- in 128-byte slots,
+    // [n_iso][2^guide_log2]; null when not built
+    const double2 *binrec;
+    int bin_prefetch;                // nuclides ahead whose bin record is prefetched into L2
     double mat_thresh[kMaterials];   // pick_mat running sums, Simulation.c:450-457
     unsigned long long mat_tseed[kMaterials];  // smallest LCG state whose draw reaches each sum
     int mat_lo[kMaterials];          // smallest / largest nuclide id of each material
@@ -99,7 +110,9 @@ struct xs_ctx {
     // tuned defaults
     int plain_tile = 1024;
     int batched_buckets = 4096;
-    int batched_blocks_per_sm = 4;
+    int batched_blocks_per_sm = 4;            // in 256-thread blocks (threads per SM / 256)
+    int plain_block = 256;                    // threads per block of the plain kernel
+    int batched_block = 256;                  // threads per block of the persistent list kernel
     int fuel_lanes = 1;                       // plain kernel, FAST: lanes per fuel lookup
     int batched_fuel_lanes = 1;               // the same for the batched kernel
     // plain kernel: material rows in shared memory (1), through the
@@ -145,6 +158,14 @@ xs_status ctx_alloc(xs_ctx *ctx, void **p, size_t bytes);
 xs_status build_derived_tables(xs_ctx *ctx);
 // the union table, when the grid is unionized and device memory allows
 xs_status build_union_table(xs_ctx *ctx);
+// the energy-bin guide of the hash / nuclide searches (part of build_derived_tables)
+xs_status build_guide(xs_ctx *ctx);
+// hash grid of `bins` bins (GridInit.c:128-151) and the nuclide grid's coarse
+// keys (every kCoarseStride-th order key), built on the device
+cudaError_t launch_hash_grid(const xs_gridpoint *grid, long n_iso, long n_gp, int bins, int *index,
+                             int sm_count, cudaStream_t st);
+cudaError_t launch_coarse_keys(const long long *ekeys, long n_iso, long n_gp, int n_coarse,
+                               long long *coarse, int sm_count, cudaStream_t st);
 
 // lookup launchers (lookup.cu).  Every launcher only enqueues on `st`.
 struct Outputs {
@@ -168,9 +189,11 @@ struct PlainScratch {
 size_t plain_scratch_bytes(long count, int tile);
 PlainScratch carve_plain_scratch(void *buf, long count, int tile);
 // ps == null: each block runs the partial chunks of its tile with idle lanes.
+// block: threads per block (128, 256 or 512; 0 = the context's, halved while
+// above the tile).
 xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                       long count, int tile, const SampleInput &in, const Outputs &out,
-                       const PlainScratch *ps, int *launches);
+                       long count, int tile, int block, const SampleInput &in,
+                       const Outputs &out, const PlainScratch *ps, int *launches);
 xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                          long count, int block, int buckets, const SampleInput &in,
                          const Outputs &out, int *launches);
@@ -201,8 +224,11 @@ xs_status enqueue_batched_in(xs_ctx *ctx, cudaStream_t st, int arith, long first
 // 1 << nb_log2) bytes); verification and error are left null for the caller.
 BatchedScratch carve_batched_scratch(void *buf, long count, int nb_log2);
 xs_status enqueue_batched_buf(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
-                              long count, int nb_log2, const SampleInput &in, const Outputs &out,
-                              const BatchedScratch &b, int *launches);
+                              long count, int nb_log2, int block, const SampleInput &in,
+                              const Outputs &out, const BatchedScratch &b, int *launches);
+// Blocks of the persistent list kernel for `block` threads each (0: the
+// context's): batched_blocks_per_sm x 256 threads per SM.
+int list_blocks(const xs_ctx *ctx, int block);
 xs_status launch_sample(xs_ctx *ctx, cudaStream_t st, long first, long count, double *E, int *mat);
 
 struct ListArgs;
