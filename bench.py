@@ -206,6 +206,175 @@ def cpu_baseline_oracle(inputs_x, problem, workload, budget_s=10.0):
             "sample": k0["sample"] + " (k0, the event loop)", "k0": k0, "k1": k1}
 
 
+# ---------------------------------------------------------- side measurements
+XL_HASH = 156835   # the reference build's XL event value (no published constant; io.c:85-106)
+
+
+def expected_hash(wl):
+    if wl["size"] == "XL":
+        return XL_HASH if wl.get("lookups") == 100000000 else None
+    return {"large": 952131, "small": 945990}.get(wl["size"])
+
+
+def profiled_dram(kernel_file, workload):
+    """DRAM bytes per lookup from a committed ncu summary (profiles/<kernel>_<workload>.md)."""
+    name = os.path.join(ROOT, "profiles", f"{kernel_file}_{workload}.md")
+    try:
+        for line in open(name):
+            if line.strip().startswith("dram_bytes_per_lookup:"):
+                return float(line.split(":", 1)[1].split()[0]), os.path.relpath(name, ROOT)
+    except OSError:
+        pass
+    return None, None
+
+
+def time_kernel(ctx, stream, n, steps, warmup, **kw):
+    """(lookups/s, ms per step, last Result) of `steps` event runs, device-timed."""
+    import torch
+    for _ in range(warmup):
+        ctx.run_event(async_=True, stream=stream, count=n, **kw)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.run_event(async_=True, stream=stream, count=n, **kw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    r = ctx.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    return n * steps / t, t / steps * 1e3, r
+
+
+def side_measurements(stream, steps, warmup, fp64_peak, peak_gbs):
+    """The other configurations of the benchmark set on this GPU, one problem
+    at a time (built on the device): the large hash grid (plain, batched,
+    forward + adjoint), the XL problem on the hash and nuclide grids (plain
+    and batched, 100,000,000 lookups), the large unionized grid batched
+    without its union table (the sort's own gain), and the reference's own
+    CUDA kernels (baseline and optimisation 6) through oracle/ref_cuda_harness."""
+    import torch
+    import xsbench_gb300 as X
+    out = {}
+
+    def plain_key(wl_name, wl, ctx, inputs, nn):
+        exp = expected_hash(wl)
+        v, ms, r = time_kernel(ctx, stream, inputs.lookups, steps, warmup, kernel="plain")
+        bpl = algorithmic_bytes_per_lookup(inputs, nn)
+        nbar = sum(p * k for p, k in zip(material_probabilities(), nn))
+        rec = {"value": v, "unit": UNIT, "ms_per_step": ms, "hash": r.hash,
+               "hash_ok": exp is None or r.hash == exp,
+               "roofline": {"bound": "hbm", "achieved": v * bpl / 1e9, "peak": peak_gbs,
+                            "unit": "GB/s", "frac": v * bpl / 1e9 / peak_gbs,
+                            "algorithmic_bytes_per_lookup": round(bpl, 1)},
+               "fp64": {"ops_per_lookup": round(11 * nbar, 1),
+                        "frac": v * 11 * nbar / fp64_peak}}
+        dram, src = profiled_dram("k_plain", wl_name)
+        if dram:
+            rec["dram"] = {"bytes_per_lookup": dram, "achieved_gbs": v * dram / 1e9,
+                           "frac": v * dram / 1e9 / peak_gbs, "source": src}
+        return rec
+
+    def batched_key(wl_name, wl, ctx, inputs, nn, ops_per_nuclide=11):
+        exp = expected_hash(wl)
+        v, ms, r = time_kernel(ctx, stream, inputs.lookups, steps, warmup, kernel="batched")
+        nbar = sum(p * k for p, k in zip(material_probabilities(), nn))
+        rec = {"value": v, "unit": UNIT, "ms_per_step": ms, "hash": r.hash,
+               "hash_ok": exp is None or r.hash == exp,
+               "fp64": {"ops_per_lookup": round(ops_per_nuclide * nbar, 1),
+                        "frac": v * ops_per_nuclide * nbar / fp64_peak}}
+        dram, src = profiled_dram("k_batched_lookup", wl_name)
+        if dram:
+            rec["dram"] = {"bytes_per_lookup": dram, "achieved_gbs": v * dram / 1e9,
+                           "frac": v * dram / 1e9 / peak_gbs, "source": src}
+        return rec
+
+    def open_ctx(wl):
+        inputs = X.make_inputs(method="event", **wl)
+        ctx = X.Context(inputs)   # built on the device
+        nn = [34 if inputs.n_isotopes == 68 else 321, 5, 4, 4, 27, 21, 21, 21, 21, 21, 9, 9]
+        return inputs, ctx, nn
+
+    # large hash grid: plain, batched, forward + adjoint
+    wl = WORKLOADS["large_hash"]
+    inputs, ctx, nn = open_ctx(wl)
+    try:
+        out["large_hash_plain"] = plain_key("large_hash", wl, ctx, inputs, nn)
+        out["large_hash_batched"] = batched_key("large_hash", wl, ctx, inputs, nn)
+        N = inputs.lookups
+        g = torch.randn((N, 5), dtype=torch.float64, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(1234))
+        d_e = torch.empty(N, dtype=torch.float64, device="cuda")
+        d_c = torch.zeros((12, 321), dtype=torch.float64, device="cuda")
+        d_x = torch.zeros((inputs.n_isotopes, inputs.n_gridpoints, 5), dtype=torch.float64,
+                          device="cuda")
+        macro = torch.empty((N, 5), dtype=torch.float64, device="cuda")
+        akw = dict(count=N, stream=stream, macro_out=macro, d_concs=d_c, d_xs=d_x, d_energy=d_e)
+        for _ in range(2):
+            ctx.adjoint(g, **akw)
+        times = [ctx.adjoint(g, **akw) for _ in range(max(3, steps // 2))]
+        t_adj = statistics.median(r.device_ms for r in times) / 1e3
+        out["large_hash_forward_adjoint"] = {
+            "value": N / t_adj, "unit": UNIT, "ms_per_step": t_adj * 1e3,
+            "vs_forward": (N / t_adj) / out["large_hash_plain"]["value"],
+            "hash_ok": times[-1].hash == 952131,
+            "what": "forward macro_xs + dL/dE + dL/dconcs + dL/dxs, device arrays, N(0,1) upstream"}
+        del g, d_e, d_c, d_x, macro
+    finally:
+        ctx.close()
+    # the XL problem on both grids
+    for name in ("xl_hash", "xl_nuclide"):
+        wl = WORKLOADS[name]
+        inputs, ctx, nn = open_ctx(wl)
+        try:
+            out[name + "_plain"] = plain_key(name, wl, ctx, inputs, nn)
+            out[name + "_batched"] = batched_key(name, wl, ctx, inputs, nn)
+        finally:
+            ctx.close()
+    # batched on the large unionized grid without the union table
+    os.environ["XSGB_UNION_TABLE"] = "0"
+    try:
+        wl = WORKLOADS["large_unionized"]
+        inputs, ctx, nn = open_ctx(wl)
+        try:
+            out["large_unionized_batched_no_union_table"] = batched_key(
+                "large_unionized_records", wl, ctx, inputs, nn)
+            out["large_unionized_batched_no_union_table"]["union_table"] = ctx.union_table_bytes > 0
+        finally:
+            ctx.close()
+    finally:
+        del os.environ["XSGB_UNION_TABLE"]
+    out["reference_cuda"] = reference_cuda_kernels()
+    return out
+
+
+def reference_cuda_kernels():
+    """The reference's cuda/Simulation.cu kernels (baseline, k0, and
+    optimisation 6, k6) on this GPU, large unionized problem: its sm_103a
+    cubin built from its sources (oracle/_ref) and launched by
+    oracle/ref_cuda_harness (device time of the lookup launches)."""
+    cubin = os.path.join(ROOT, "oracle", "_ref", "xsbench_cuda_sim.cubin")
+    if not os.path.exists(cubin):
+        return {"unavailable": "the reference's CUDA cubin (oracle/_ref) was not built for this run"}
+    exe = os.path.join(ROOT, "oracle", "_build", "ref_cuda_harness")
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "harness"],
+                       capture_output=True, text=True)
+    if r.returncode != 0 or not os.path.exists(exe):
+        return {"unavailable": "oracle/ref_cuda_harness did not build: " + (r.stderr or r.stdout)[-200:]}
+    res = {}
+    for k in (0, 6):
+        r = subprocess.run([exe, "-m", "event", "-s", "large", "-G", "unionized", "-k", str(k),
+                            "--reps", "3", "--cubin", cubin], capture_output=True, text=True,
+                           cwd=ROOT, timeout=600)
+        try:
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            res[f"k{k}"] = {"value": d["lookups_per_s"], "unit": UNIT, "ms": d["ms"],
+                            "what": d["what"], "hash_ok": d["hash"] == 952131}
+        except Exception:
+            res[f"k{k}"] = {"unavailable": (r.stderr or r.stdout)[-200:]}
+    return res
+
+
 # ------------------------------------------------------------- reference arm
 def reference_arm(args, rank):
     """The reference's own CPU implementation of the path on the host cores:
@@ -304,6 +473,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the side measurement of the other kernel on the same workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the other configurations (large hash, XL, no union table, reference CUDA)")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -498,8 +669,12 @@ def main():
             "clocks": clk,
             "cpu_baseline": cpu,
         }
+    ctx.close()   # frees the device for the side configurations
+    if rank == 0 and world == 1 and not args.no_side and not args.gridpoints \
+            and args.workload == "large_unionized":
+        line["side"] = side_measurements(stream, max(3, min(args.steps, 5)), 3, fp64_peak, peak)
+    if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     problem.close()
     if dist:
         dist.destroy_process_group()

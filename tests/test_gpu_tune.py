@@ -12,7 +12,7 @@ from conftest import golden_json, product_inputs
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_nuclide"])
+@pytest.mark.parametrize("name", ["tiny_unionized", "tiny_nuclide", "tiny_hash"])
 def test_autotune_keeps_results_and_caches(tmp_path, name):
     g = golden_json("full_" + name)
     cache = str(tmp_path / "tune.json")
@@ -33,6 +33,7 @@ def test_autotune_keeps_results_and_caches(tmp_path, name):
         assert val["lookups_per_s"] > 0
         assert val["fuel_lanes"] in (1, 2, 4)
         assert val["block"] == best["block"] in (128, 256, 512)
+        assert val["guided"] in (0, 1) and val["tile_sort"] in (-1, 0, 1)
         with X.Context(inp, p) as ctx2:
             t0 = time.perf_counter()
             best2 = ctx2.autotune(cache)

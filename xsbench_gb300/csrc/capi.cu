@@ -399,6 +399,7 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
         if (v == 1 || v == 2 || v == 4) ctx->fuel_lanes = v;
     }
     if (const char *env = getenv("XSGB_STAGE_ROWS")) ctx->stage_rows = atoi(env) != 0 ? 1 : 0;
+    if (const char *env = getenv("XSGB_TILE_SORT")) ctx->tile_sort = atoi(env) != 0 ? 1 : 0;
     if (const char *env = getenv("XSGB_BATCHED_FUEL_LANES")) {
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->batched_fuel_lanes = v;
@@ -442,6 +443,9 @@ xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, x
     }
     ctx->base_coarse = t.coarse;
     ctx->base_n_coarse = t.n_coarse;
+    ctx->own_guide = t.guide;
+    ctx->own_binrec = t.binrec;
+    ctx->base_guided = t.guide != nullptr;
     *out = ctx;
     return XS_OK;
 }

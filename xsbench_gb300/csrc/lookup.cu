@@ -253,6 +253,7 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
     if (tile > 8192) return fail(XS_ERR_INVALID_ARGUMENT, "tile_lookups %d above 8192", tile);
     PlainArgs a;
     a.block = block;
+    a.esort = ctx->tile_sort >= 0 ? ctx->tile_sort : ctx->t.grid_type != XS_UNIONIZED;
     a.first = first;
     a.count = count;
     a.tile = tile;

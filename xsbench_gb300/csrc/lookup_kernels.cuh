@@ -41,7 +41,22 @@ struct PlainArgs {
     int stage_rows;
     int rows_total;
     int block;                   // threads per block: 128, 256 or 512 (tile a multiple of it)
+    // 1: within each material the tile's lookups are also ordered by energy
+    // (kTileBuckets buckets over [0, 1)), so a warp's lookups lie in a narrow
+    // energy window and its loads of a nuclide's table touch few pages
+    int esort;
 };
+
+constexpr int kTileBucketsLog2 = 6;
+constexpr int kTileBuckets = 1 << kTileBucketsLog2;   // energy buckets of the in-tile sort
+
+// Energy bucket of the in-tile sort: floor(E * kTileBuckets) on [0, 1), the
+// end buckets outside it (NaN: 0).
+__device__ __forceinline__ int tile_bucket(double E)
+{
+    if (E >= 0.0 && E < 1.0) return xsgb_floor_scaled_pow2(E, kTileBucketsLog2);
+    return E >= 1.0 ? kTileBuckets - 1 : 0;
+}
 
 // A material-segmented list of lookups (the batched sort, or the plain
 // kernel's overflow).  Chunk c covers virtual positions [32c, 32c+32); the
@@ -241,6 +256,14 @@ __global__ void __launch_bounds__(BLOCK, XSGB_PLAIN_MIN_BLOCKS * kBlock / BLOCK)
     const int tid = threadIdx.x;
     const long base = (long)blockIdx.x * tile;
     const int ntile = (int)min((long)tile, a.count - base);
+    // the in-tile energy sort's counts and cursors, after everything else
+    int *hcnt = nullptr;
+    if (a.esort) {
+        const size_t o_rows = ((size_t)tile * 13 + kMaterials * 128 + 7) & ~(size_t)7;
+        hcnt = reinterpret_cast<int *>(smem + ((o_rows + (SROW ? (size_t)a.rows_total * 12 : 0) + 3) &
+                                               ~(size_t)3));
+        for (int i = tid; i < kMaterials * kTileBuckets; i += BLOCK) hcnt[i] = 0;
+    }
     if (tid < kMaterials) cnt[tid] = 0;
     if (tid == 0) {
         qhead = 0;
@@ -259,7 +282,10 @@ __global__ void __launch_bounds__(BLOCK, XSGB_PLAIN_MIN_BLOCKS * kBlock / BLOCK)
             bool ok = sample_at<true>(t, a.in_E, a.in_mat, base + l, seed, E, m, a.err);
             sE[l] = E;
             sMat[l] = ok ? (unsigned char)m : 0xFF;
-            if (ok) atomicAdd(&cnt[m], 1);
+            if (ok) {
+                atomicAdd(&cnt[m], 1);
+                if (hcnt) atomicAdd(&hcnt[m * kTileBuckets + tile_bucket(E)], 1);
+            }
         }
     } else {
         const int l0 = tid * lpt;
@@ -273,6 +299,7 @@ __global__ void __launch_bounds__(BLOCK, XSGB_PLAIN_MIN_BLOCKS * kBlock / BLOCK)
                 sE[l0 + q] = E;
                 sMat[l0 + q] = (unsigned char)m;
                 atomicAdd(&cnt[m], 1);
+                if (hcnt) atomicAdd(&hcnt[m * kTileBuckets + tile_bucket(E)], 1);
             }
         }
     }
@@ -292,9 +319,26 @@ __global__ void __launch_bounds__(BLOCK, XSGB_PLAIN_MIN_BLOCKS * kBlock / BLOCK)
         obase[tid] = rem ? atomicAdd(&a.ovf_cnt[tid], rem) : 0;
     }
     __syncthreads();
-    for (int l = tid; l < ntile; l += BLOCK) {
-        int m = sMat[l];
-        if (m != 0xFF) perm[atomicAdd(&cur[m], 1)] = l;
+    if (hcnt) {
+        // each material's buckets start where the previous one's end
+        if (tid < kMaterials) {
+            int run = seg[tid];
+            for (int b = 0; b < kTileBuckets; b++) {
+                const int c = hcnt[tid * kTileBuckets + b];
+                hcnt[tid * kTileBuckets + b] = run;
+                run += c;
+            }
+        }
+        __syncthreads();
+        for (int l = tid; l < ntile; l += BLOCK) {
+            int m = sMat[l];
+            if (m != 0xFF) perm[atomicAdd(&hcnt[m * kTileBuckets + tile_bucket(sE[l])], 1)] = l;
+        }
+    } else {
+        for (int l = tid; l < ntile; l += BLOCK) {
+            int m = sMat[l];
+            if (m != 0xFF) perm[atomicAdd(&cur[m], 1)] = l;
+        }
     }
     __syncthreads();
     if (overflow) {
@@ -531,10 +575,17 @@ __global__ void __launch_bounds__(kBlock) k_history(Tables t, long first, long c
 }
 
 // ------------------------------------------------------------ launchers ---
-inline size_t plain_smem_bytes(int tile, int rows_total = 0)
+inline size_t plain_smem_bytes(int tile, int rows_total = 0, bool esort = false)
 {
+    // the kernel's layout: tile arrays (b bytes); from the next 8-byte
+    // boundary the staged rows (rows_total entries); from the next 4-byte
+    // boundary the sort histogram
     const size_t b = (size_t)tile * 8 + (size_t)(tile + kMaterials * 32) * 4 + tile;
-    return rows_total ? ((b + 7) & ~(size_t)7) + (size_t)rows_total * 12 : b;
+    const size_t o_rows = (b + 7) & ~(size_t)7;
+    if (esort)
+        return ((o_rows + (size_t)rows_total * 12 + 3) & ~(size_t)3) +
+               (size_t)kMaterials * kTileBuckets * 4;
+    return rows_total ? o_rows + (size_t)rows_total * 12 : b;
 }
 
 template <int GRID>
@@ -547,8 +598,8 @@ struct GridLaunch {
         // the others keep the smaller shared-memory carveout (and their L1)
         const bool srow = a.stage_rows && a.rows_total > 0 && !checked &&
                           arith != XS_ARITH_EXACT &&
-                          plain_smem_bytes(a.tile, a.rows_total) <= 96 * 1024;
-        const size_t sm = plain_smem_bytes(a.tile, srow ? a.rows_total : 0);
+                          plain_smem_bytes(a.tile, a.rows_total, a.esort) <= 96 * 1024;
+        const size_t sm = plain_smem_bytes(a.tile, srow ? a.rows_total : 0, a.esort);
         // shared-memory share of the SM's 228 KB that holds the resident
         // blocks (each with its static arrays and 1 KB reserved), L1 the rest
         // (the resident blocks: XSGB_PLAIN_MIN_BLOCKS of 256 threads, or as

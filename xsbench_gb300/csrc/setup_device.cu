@@ -351,6 +351,9 @@ extern "C" xs_status xs_ctx_create_on_device(const xs_inputs *in, int device, xs
     }
     ctx->base_coarse = t.coarse;
     ctx->base_n_coarse = t.n_coarse;
+    ctx->own_guide = t.guide;
+    ctx->own_binrec = t.binrec;
+    ctx->base_guided = t.guide != nullptr;
     *out = ctx;
     return XS_OK;
 }

@@ -26,15 +26,18 @@ struct GridView {
     const int *index_grid;
     const long long *coarse;
     int n_coarse;
+    int guided;          // 1: the guided searches (energy-bin guide and bin records)
 };
 
 static GridView view_of(const Tables &t)
 {
-    return GridView{t.grid_type, t.hash_bins, t.hash_du, t.index_grid, t.coarse, t.n_coarse};
+    return GridView{t.grid_type, t.hash_bins, t.hash_du, t.index_grid, t.coarse, t.n_coarse,
+                    t.guide != nullptr};
 }
 
-static void apply_view(Tables &t, const GridView &v)
+static void apply_view(xs_ctx *ctx, const GridView &v)
 {
+    Tables &t = ctx->t;
     t.grid_type = v.grid_type;
     t.hash_bins = v.hash_bins;
     t.hash_du = v.hash_du;
@@ -42,6 +45,8 @@ static void apply_view(Tables &t, const GridView &v)
     t.index_grid = v.index_grid;
     t.coarse = v.coarse;
     t.n_coarse = v.n_coarse;
+    t.guide = v.guided ? ctx->own_guide : nullptr;
+    t.binrec = v.guided ? ctx->own_binrec : nullptr;
 }
 
 static std::string cache_key(const xs_ctx *ctx)
@@ -60,6 +65,8 @@ struct Choice {
     int grid_type = -1, kernel = 0, tile = 1024, buckets = 4096, blocks_per_sm = 4, lanes = 1;
     double rate = 0;
     int block = 256;   // threads per block of the chosen kernel
+    int guided = 0;    // the guided searches (hash / nuclide grids)
+    int tile_sort = 0; // plain kernel: energy order within each tile's materials
 };
 
 // cache file: one entry per line, {"<key>": {...}} inside a JSON object
@@ -76,9 +83,9 @@ static bool cache_read(const char *path, const std::string &key, Choice &c)
         p += want.size();
         if (sscanf(p, " {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
                       "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"block\": %d, "
-                      "\"lookups_per_s\": %lf",
+                      "\"guided\": %d, \"tile_sort\": %d, \"lookups_per_s\": %lf",
                    &c.grid_type, &c.kernel, &c.tile, &c.buckets, &c.blocks_per_sm, &c.lanes,
-                   &c.block, &c.rate) == 8 &&
+                   &c.block, &c.guided, &c.tile_sort, &c.rate) == 10 &&
             (c.lanes == 1 || c.lanes == 2 || c.lanes == 4) &&
             (c.block == 128 || c.block == 256 || c.block == 512) && c.tile % c.block == 0)
             found = true;
@@ -105,9 +112,10 @@ static void cache_write(const char *path, const std::string &key, const Choice &
     char buf[1024];
     snprintf(buf, sizeof buf,
              "  \"%s\": {\"grid_type\": %d, \"kernel\": %d, \"tile\": %d, \"buckets\": %d, "
-             "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"block\": %d, \"lookups_per_s\": %.6g}",
+             "\"blocks_per_sm\": %d, \"fuel_lanes\": %d, \"block\": %d, \"guided\": %d, "
+             "\"tile_sort\": %d, \"lookups_per_s\": %.6g}",
              key.c_str(), c.grid_type, c.kernel, c.tile, c.buckets, c.blocks_per_sm, c.lanes,
-             c.block, c.rate);
+             c.block, c.guided, c.tile_sort, c.rate);
     lines.push_back(buf);
     FILE *f = fopen(path, "w");
     if (!f) return;
@@ -129,10 +137,10 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
     // the grid types this context can serve, starting with the one it was built with
     const GridView base{ctx->inputs.grid_type, ctx->inputs.hash_bins,
                         ctx->inputs.hash_bins > 0 ? 1.0 / ctx->inputs.hash_bins : 0.0,
-                        ctx->own_index, ctx->base_coarse, ctx->base_n_coarse};
-    apply_view(t, base);
+                        ctx->own_index, ctx->base_coarse, ctx->base_n_coarse,
+                        ctx->base_guided};
+    apply_view(ctx, base);
     std::vector<GridView> views;
-    views.push_back(base);
     if (!ctx->tune_hash_index && t.grid_type != XS_HASH) {
         void *p = nullptr;
         const int bins = 10000;
@@ -151,16 +159,32 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         ctx->tune_coarse = (long long *)p;
         ctx->tune_n_coarse = nc;
     }
-    if (!t.guide) {   // the guided searches of the hash and nuclide grids
+    if (!ctx->own_guide) {   // the guided searches of the hash and nuclide grids
         xs_status s = build_guide(ctx);
         if (s != XS_OK) return s;
+        ctx->own_guide = t.guide;
+        ctx->own_binrec = t.binrec;
     }
+    // every grid type the context can serve; the hash and nuclide grids both
+    // with and without the guided searches (when the guide could be built)
+    std::vector<GridView> grids{base};
     if (base.grid_type != XS_HASH)
-        views.push_back(GridView{XS_HASH, 10000, 1.0 / 10000, ctx->tune_hash_index, base.coarse,
-                                 base.n_coarse});
+        grids.push_back(GridView{XS_HASH, 10000, 1.0 / 10000, ctx->tune_hash_index, base.coarse,
+                                 base.n_coarse, 0});
     if (base.grid_type != XS_NUCLIDE)
-        views.push_back(GridView{XS_NUCLIDE, base.hash_bins, base.hash_du, base.index_grid,
-                                 ctx->tune_coarse, ctx->tune_n_coarse});
+        grids.push_back(GridView{XS_NUCLIDE, base.hash_bins, base.hash_du, base.index_grid,
+                                 ctx->tune_coarse, ctx->tune_n_coarse, 0});
+    for (GridView v : grids) {
+        if (v.grid_type == XS_UNIONIZED || !ctx->own_guide) {
+            v.guided = 0;
+            views.push_back(v);
+            continue;
+        }
+        v.guided = 1;
+        views.push_back(v);
+        v.guided = 0;
+        views.push_back(v);
+    }
     XS_CUDA(cudaStreamSynchronize(ctx->stream));
 
     const std::string key = cache_key(ctx);
@@ -186,8 +210,10 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         const int saved_bps = ctx->batched_blocks_per_sm;
         const int saved_lanes = ctx->fuel_lanes, saved_blanes = ctx->batched_fuel_lanes;
         const int saved_pblock = ctx->plain_block, saved_bblock = ctx->batched_block;
+        const int saved_sort = ctx->tile_sort;
         auto restore = [&]() {
-            apply_view(t, original);
+            apply_view(ctx, original);
+            ctx->tile_sort = saved_sort;
             ctx->batched_blocks_per_sm = saved_bps;
             ctx->fuel_lanes = saved_lanes;
             ctx->batched_fuel_lanes = saved_blanes;
@@ -197,7 +223,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         // the shapes are searched at 256 threads per block, the block size after
         ctx->plain_block = ctx->batched_block = 256;
         for (const GridView &v : views) {
-            apply_view(t, v);
+            apply_view(ctx, v);
             for (int bps : {3, 4}) {
                 ctx->batched_blocks_per_sm = bps;
                 for (int lanes : {1, 2, 4}) {
@@ -214,7 +240,9 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                             restore();
                             return s;
                         }
-                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, lanes, rate, 256};
+                        if (rate > c.rate)
+                            c = Choice{v.grid_type, XS_KERNEL_PLAIN, tile, c.buckets, bps, lanes, rate,
+                                       256, v.guided, -1};
                     }
                     for (int nb : {256, 1024, 4096, 16384}) {
                         xs_run_opts o;
@@ -228,7 +256,9 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                             restore();
                             return s;
                         }
-                        if (rate > c.rate) c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, lanes, rate, 256};
+                        if (rate > c.rate)
+                            c = Choice{v.grid_type, XS_KERNEL_BATCHED, c.tile, nb, bps, lanes, rate,
+                                       256, v.guided, -1};
                     }
                 }
             }
@@ -237,7 +267,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
         // place and the threads per SM unchanged (the plain kernel's blocks
         // divide its tile)
         for (const GridView &v : views)
-            if (v.grid_type == c.grid_type) apply_view(t, v);
+            if (v.grid_type == c.grid_type && v.guided == c.guided) apply_view(ctx, v);
         ctx->batched_blocks_per_sm = c.blocks_per_sm;
         ctx->fuel_lanes = c.lanes;
         ctx->batched_fuel_lanes = c.lanes;
@@ -261,18 +291,41 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                 c.block = block;
             }
         }
+        // the plain kernel's in-tile energy order, on and off (the search
+        // above ran the grid type's default)
+        if (c.kernel == XS_KERNEL_PLAIN) {
+            ctx->plain_block = c.block;
+            for (int ts : {0, 1}) {
+                ctx->tile_sort = ts;
+                xs_run_opts o;
+                xs_run_opts_init(&o);
+                o.count = sample;
+                o.tile_lookups = c.tile;
+                double rate = 0;
+                xs_status s = time_run(o, &rate);
+                if (s != XS_OK) {
+                    restore();
+                    return s;
+                }
+                if (rate > c.rate) {
+                    c.rate = rate;
+                    c.tile_sort = ts;
+                }
+            }
+        }
         restore();
         if (cache_path) cache_write(cache_path, key, c);
     }
     // install the choice
     for (const GridView &v : views)
-        if (v.grid_type == c.grid_type) apply_view(t, v);
+        if (v.grid_type == c.grid_type && v.guided == c.guided) apply_view(ctx, v);
     ctx->plain_tile = c.tile;
     ctx->batched_buckets = c.buckets;
     ctx->batched_blocks_per_sm = c.blocks_per_sm;
     if (c.kernel == XS_KERNEL_PLAIN) {
         ctx->fuel_lanes = c.lanes;
         ctx->plain_block = c.block;
+        if (c.tile_sort >= 0) ctx->tile_sort = c.tile_sort;
     } else {
         ctx->batched_fuel_lanes = c.lanes;
         ctx->batched_block = c.block;

@@ -119,6 +119,9 @@ struct xs_ctx {
     // read-only cache (0), or by grid type (-1: staged on the unionized grid,
     // +0.7 % there; 0.4 % slower on the hash grid, even on the nuclide grid)
     int stage_rows = -1;
+    // plain kernel: tile lookups ordered by energy within each material (1),
+    // by material only (0), or by grid type (-1: on the hash and nuclide grids)
+    int tile_sort = -1;
     int num_nucs_host[xsgb::kMaterials] = {}; // host copy of num_nucs
     size_t union_table_bytes = 0;             // 0: no union table
     std::map<std::string, xsgb::BatchedGraph> graphs;
@@ -138,6 +141,11 @@ struct xs_ctx {
     int *tune_hash_index = nullptr;           // derived 10,000-bin hash grid
     long long *tune_coarse = nullptr;         // derived coarse keys (nuclide grid)
     int tune_n_coarse = 0;
+    // the guided searches' tables (owned through `allocations`); the tuner
+    // may switch them off for a grid view
+    const int *own_guide = nullptr;
+    const double2 *own_binrec = nullptr;
+    int base_guided = 0;                      // built with the context
 };
 
 namespace xsgb {
