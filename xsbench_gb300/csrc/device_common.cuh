@@ -879,8 +879,12 @@ __device__ __forceinline__ void macro_xs(const Tables &t, double E, int mat, dou
     if (ARITH == XS_ARITH_FAST && t.binrec &&
         macro_xs_binned<GRID, CHECKED, DE, SROW>(t, E, n, mrow, crow, macro, err, S, q0, stride))
         return;
-    if (t.guide && macro_xs_guided<GRID, ARITH, CHECKED, DE, SROW>(t, E, n, mrow, crow, macro, err,
-                                                                    S, q0, stride))
+    // (FAST arithmetic without bin records -- a device short of memory for
+    // them -- keeps the grid's own search: one register set less in the
+    // FAST kernels)
+    if (ARITH == XS_ARITH_EXACT && t.guide &&
+        macro_xs_guided<GRID, ARITH, CHECKED, DE, SROW>(t, E, n, mrow, crow, macro, err, S, q0,
+                                                        stride))
         return;
     long row = 0;
     long long q = 0;

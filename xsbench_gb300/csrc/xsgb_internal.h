@@ -122,6 +122,11 @@ struct xs_ctx {
     // plain kernel: tile lookups ordered by energy within each material (1),
     // by material only (0), or by grid type (-1: on the hash and nuclide grids)
     int tile_sort = -1;
+    // plain kernel over the event batch: the tiles' partial 32-lookup chunks
+    // run in a second, packed pass (1), padded in their tiles (0), or by grid
+    // type (-1: the pass runs except on the nuclide grid without the guided
+    // searches)
+    int overflow = -1;
     int num_nucs_host[xsgb::kMaterials] = {}; // host copy of num_nucs
     size_t union_table_bytes = 0;             // 0: no union table
     std::map<std::string, xsgb::BatchedGraph> graphs;
