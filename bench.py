@@ -110,8 +110,12 @@ def profiled_traffic(workload, kernel):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from
+    start() (before the end of the warm-up, so that the sampler is running
+    when the timed region begins) to stop(); only the samples stamped inside
+    the timed region [mark_begin(), mark_end()] are reported (all of them if
+    none is)."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -119,16 +123,31 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.f = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+
+    def mark_begin(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
 
     def stop(self):
         if self.proc is None:
@@ -142,21 +161,23 @@ class ClockSampler:
         self.f.seek(0)
         rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
-        sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        samples = []
         for r in rows:
             try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-                for n, v in zip(names, r[5:9]):
-                    if v.strip().lower() == "active":
-                        reasons.add(n)
+                samples.append((self._stamp(r[0]), float(r[2]), float(r[3]),
+                                {n for n, v in zip(names, r[6:10]) if v.strip().lower() == "active"}))
             except (ValueError, IndexError):
                 continue
-        if not sm:
+        inside = [x for x in samples if x[0] is not None and self.t0 is not None
+                  and self.t1 is not None and self.t0 - 0.05 <= x[0] <= self.t1 + 0.05]
+        used = inside or samples
+        if not used:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        return {"sm_mhz": statistics.median(x[1] for x in used),
+                "sm_max_mhz": max(x[2] for x in used), "samples": len(used),
+                "in_timed_region": bool(inside),
+                "reasons": sorted(set().union(*(x[3] for x in used)))}
 
 
 def cpu_k1(L, inp, sd, lookups, cores, budget_s):
@@ -410,11 +431,16 @@ def reference_arm(args, rank):
         L = oracle.lib()
         run = lambda a, n: L.or_run_event(C.byref(prob.inp), C.byref(prob.sd), a, n, cores,  # noqa: E731
                                           None, None, None, None)
-    # a bounded sample per step: about 2 s of work at the measured rate
+    # each step the whole batch when the run (warm-up + timed steps) fits in
+    # about 150 s at the measured rate -- the same workload as the GPU arm's
+    # step -- else a bounded sample of about 2 s of work per step
     t0 = time.perf_counter()
     run(0, 100000)
     rate0 = 100000 / (time.perf_counter() - t0)
-    per_step = int(min(inp.lookups // max(1, args.steps), max(100000, rate0 * 2.0)))
+    if inp.lookups * (args.steps + args.warmup) / rate0 <= 150.0:
+        per_step = inp.lookups
+    else:
+        per_step = int(min(inp.lookups // max(1, args.steps), max(100000, rate0 * 2.0)))
     for s in range(args.warmup):
         run(s * per_step % max(1, inp.lookups - per_step), per_step)
     t0 = time.perf_counter()
@@ -440,7 +466,8 @@ def reference_arm(args, rank):
         "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (the reference's LCG generators)",
         "config": {"workload": args.workload, "kernel": "openmp-threading event loop (k0)",
-                   "sample_lookups_per_step": per_step},
+                   "sample_lookups_per_step": per_step,
+                   "whole_batch_per_step": per_step == inp.lookups},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": f"{per_step} consecutive lookups of {args.workload} per step "
                                    "(k0, the event loop)",
@@ -520,6 +547,8 @@ def main():
     # second: a freshly started GPU ran the first ~20 steps measurably slower
     # (3 warm-up steps: 849-863 M lookups/s in the first process on a box,
     # 893 M in the next; 60 warm-up steps: 893 M in the first)
+    clocks = ClockSampler(local)
+    clocks.start()   # past its start-up by the time the timed region begins
     warm, t_warm = 0, time.perf_counter()
     while warm < args.warmup or (time.perf_counter() - t_warm < 1.0 and warm < 200):
         ctx.run_event(async_=True, **kw)
@@ -528,17 +557,17 @@ def main():
 
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(local)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
+    clocks.mark_begin()
     launches = 0
     ev0.record(stream)
     for _ in range(args.steps):
         launches += ctx.run_event(async_=True, **kw).kernel_launches
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark_end()
     clk = clocks.stop()
     last = ctx.sync()
     if dist:
