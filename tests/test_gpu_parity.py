@@ -357,6 +357,78 @@ def test_edge_energies_against_oracle(name, kernel, arith):
         assert rel_err(macro[rows], ref["macro"][rows]) <= REL_TOL
 
 
+_EDGE_CACHE = {}
+
+
+def edge_samples(name):
+    """Edge energies of the hash / nuclide problem (as above, without the
+    out-of-range ones on the hash grid) and the oracle's results for them."""
+    if name not in _EDGE_CACHE:
+        rng = np.random.default_rng(23)
+        with oracle.Problem(oracle_config(name)) as o:
+            grid = np.array(o.arrays()["nuclide_grid"]).reshape(-1, 6)[:, 0]
+            edges = np.arange(500) / 500.0
+            k = 2.0 ** -12   # the guide's bin edges for 1,000 points per nuclide
+            gedges = np.arange(1, 4096) * k
+            E = [np.array([0.0, 5e-324, 1e-300, 1.0 - 2.0 ** -53]),
+                 grid[rng.integers(0, grid.size, 3000)], edges, np.nextafter(edges[1:], 0.0),
+                 gedges[rng.integers(0, gedges.size, 500)],
+                 np.nextafter(gedges[rng.integers(0, gedges.size, 500)], 0.0), rng.random(2000)]
+            if name != "tiny_hash":
+                E.append(np.array([1.0, 1.5, -0.25, 1e10, -1e10, np.nan, np.inf]))
+            E = np.concatenate(E)
+            M = rng.integers(0, 12, E.size).astype(np.int32)
+            _EDGE_CACHE[name] = (E, M, o.run_samples(E, M))
+    return _EDGE_CACHE[name]
+
+
+GUIDED_VARIANTS = [
+    {"XSGB_GUIDE": "1"},
+    {"XSGB_GUIDE": "1", "XSGB_GUIDE_LOG2": "6"},
+    {"XSGB_GUIDE": "1", "XSGB_BIN_RECORDS": "0"},
+    {"XSGB_GUIDE": "1", "XSGB_BIN_RECORDS": "0", "XSGB_GUIDE_LOG2": "6"},
+    {"XSGB_GUIDE": "1", "XSGB_TILE_SORT": "0", "XSGB_OVERFLOW": "0", "XSGB_BIN_PREFETCH": "0"},
+    {"XSGB_GUIDE": "1", "XSGB_OVERFLOW": "1", "XSGB_BIN_PREFETCH": "4", "XSGB_FUEL_LANES": "4"},
+    {"XSGB_GUIDE": "0", "XSGB_TILE_SORT": "1"},
+]
+
+
+@pytest.mark.parametrize("name", ["tiny_hash", "tiny_nuclide"])
+@pytest.mark.parametrize("variant", range(len(GUIDED_VARIANTS)))
+def test_guided_search_variants(monkeypatch, name, variant):
+    """The plain kernel's interval searches in every configuration the
+    switches select -- the guide with and without bin records, with 64 bins
+    per nuclide (about 16 gridpoints per bin, so most lookups take the walk
+    past the bin's first interval), the in-tile energy order and the overflow
+    pass on and off, prefetch distances, lanes per fuel lookup, the grids'
+    own searches -- on the hash and nuclide grids: the event batch's
+    verification sum and argmax vector against the reference's digests, and
+    the edge energies (gridpoints, hash-bin and guide-bin edges, zero,
+    subnormals) against the oracle, in both arithmetics."""
+    for k, v in GUIDED_VARIANTS[variant].items():
+        monkeypatch.setenv(k, v)
+    g = golden_json("full_" + name)
+    E, M, ref = edge_samples(name)
+    inp = product_inputs(name)
+    with X.grid_init(inp) as prob, X.Context(inp, prob) as ctx:
+        for arith in ("fast", "exact"):
+            r, _, idx = run(ctx, g["lookups"], kernel="plain", arith=arith)
+            assert r.verification == g["verification"], arith
+            assert sha(idx) == g["sha256_max_idx"], arith
+            macro = np.empty((E.size, 5))
+            mi = np.empty(E.size, np.uint8)
+            r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=mi, kernel="plain", arith=arith)
+            assert r.verification == ref["verification"], arith
+            assert np.array_equal(mi, ref["max_idx"]), arith
+            fin = np.isfinite(ref["macro"])
+            assert np.array_equal(macro[~fin], ref["macro"][~fin], equal_nan=True)
+            if arith == "exact":
+                assert np.array_equal(macro[fin], ref["macro"][fin])
+            else:
+                rows = fin.all(axis=1)
+                assert rel_err(macro[rows], ref["macro"][rows]) <= REL_TOL
+
+
 def test_drop_in_seam():
     g = golden_json("full_tiny_unionized")
     inp = product_inputs("tiny_unionized")
