@@ -786,9 +786,9 @@ __device__ __forceinline__ bool macro_xs_guided(const Tables &t, double E, int n
 // The same intervals through the bin records (Tables::binrec, FAST): slot
 // (nuc, b) already holds the record of the interval the guided search starts
 // at, so the lane reads it at an address it knows without a load -- no
-// dependent read precedes the record -- and reads the guide and walks on only
-// when E lies at or past that interval's upper gridpoint (about one nuclide
-// in ten with four bins per gridpoint).  The bin records of the nuclides
+// dependent read precedes the record -- and walks on from that interval's
+// index (kept in the slot's fourth sector) only when E lies at or past its
+// upper gridpoint (about one nuclide in ten with four bins per gridpoint).  The bin records of the nuclides
 // t.bin_prefetch ahead are prefetched into L2.
 __device__ __forceinline__ const double *binrec_at(const Tables &t, int nuc, int b)
 {
@@ -824,8 +824,9 @@ __device__ __forceinline__ bool macro_xs_binned(const Tables &t, double E, int n
         ld_v4(r + 4, v[4], v[5], v[6], v[7], pol);
         ld_v4(r + 8, v[8], v[9], v[10], v[11], pol);
         if (!(E < v[0])) {
-            // E at or past the bin's first interval: from there, through the guide
-            long k = min(max((long)ld_guide(&t.guide[(long)nuc * ((1L << t.guide_log2) + 1) + b]) - 1, 0L), top);
+            // E at or past the bin's first interval: walk on from its index,
+            // kept in the slot's fourth sector (same 128-byte line)
+            long k = (long)ldg(reinterpret_cast<const long long *>(r + 12));
             while (k < top && !(E < v[0])) {
                 k++;
                 load_interval<XS_ARITH_FAST>(t, nuc, k, v);

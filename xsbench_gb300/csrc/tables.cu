@@ -108,7 +108,10 @@ __global__ void k_guide(const xs_gridpoint *grid, long n_iso, long n_gp, int k, 
 }
 
 // Bin records: slot (nuc, b) = the record of interval
-// clamp(guide[nuc][b] - 1, 0, n_gp - 2).
+// k0 = clamp(guide[nuc][b] - 1, 0, n_gp - 2), and in the slot's fourth
+// sector (double 12, as integer bits) k0 itself, which the lookup reads only
+// when E lies past that interval: the sector comes with the slot's 128-byte
+// line, so the walk starts without a guide read.
 __global__ void k_bin_records(const double2 *rec, const int *guide, long n_iso, long n_gp, int k,
                               double2 *out)
 {
@@ -122,7 +125,9 @@ __global__ void k_bin_records(const double2 *rec, const int *guide, long n_iso, 
         const double2 *src = rec + (nuc * (n_gp - 1) + k0) * kRecordPairs;
         double2 *dst = out + i * kRecordPairs;
 #pragma unroll
-        for (int q = 0; q < kRecordPairs; q++) dst[q] = src[q];
+        for (int q = 0; q < 6; q++) dst[q] = src[q];
+        dst[6] = make_double2(__longlong_as_double((long long)k0), 0.0);
+        dst[7] = make_double2(0.0, 0.0);
     }
 }
 

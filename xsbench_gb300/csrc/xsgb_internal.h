@@ -54,9 +54,10 @@ struct Tables {
     const int *guide;
     int guide_log2;
     // bin records (FAST): for nuclide nuc and guide bin b, a copy of the
-    // interval record of interval clamp(guide[nuc][b] - 1, 0, n_gp - 2) -- the
-    // interval holding the bin's lower edge -- in 128-byte slots,
-    // [n_iso][2^guide_log2]; null when not built
+    // interval record of interval k0 = clamp(guide[nuc][b] - 1, 0, n_gp - 2) --
+    // the interval holding the bin's lower edge -- and k0 itself (double 12
+    // of the slot, integer bits), in 128-byte slots, [n_iso][2^guide_log2];
+    // null when not built
     const double2 *binrec;
     int bin_prefetch;                // nuclides ahead whose bin record is prefetched into L2
     double mat_thresh[kMaterials];   // pick_mat running sums, Simulation.c:450-457
