@@ -469,8 +469,18 @@ __device__ __forceinline__ void list_lookup_body(const Tables &t, const ListArgs
     block_verification(mine, &s_acc, a.verif);
 }
 
+// Resident threads per SM held to those of four 256-thread blocks (three on
+// the hash grid, whose search needs more registers): the sorted batches'
+// warp-cooperative searches are latency-bound (the hash grid's at 96
+// registers, two blocks per SM, ran 11-17 % slower; the nuclide grid's at 78,
+// three blocks, 17 % slower than at 64, four).
+constexpr int list_min_blocks(int grid, int block)
+{
+    return ((grid == XS_HASH ? 3 : 4) * kBlock + block - 1) / block;
+}
+
 template <int GRID, int ARITH, bool CHECKED, int BLOCK = kBlock>
-__global__ void __launch_bounds__(BLOCK) k_list_lookup(Tables t, ListArgs a)
+__global__ void __launch_bounds__(BLOCK, list_min_blocks(GRID, BLOCK)) k_list_lookup(Tables t, ListArgs a)
 {
     list_lookup_body<GRID, ARITH, CHECKED, false>(t, a);
 }

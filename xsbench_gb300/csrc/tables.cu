@@ -244,8 +244,12 @@ xs_status build_union_table(xs_ctx *ctx)
 
 // The energy-bin guide (Tables::guide) and the bin records
 // (Tables::binrec): about four bins per gridpoint (2^(ceil(log2 n_gp) + 2),
-// at most 2^26 per nuclide), so most bins hold no gridpoint and a lookup's
-// interval is the bin's first one.  Built for the hash and nuclide grids (and
+// at most 2^26 per nuclide; two where the device lacks the room), so most
+// bins hold no gridpoint and a lookup's interval is the bin's first one.
+// Measured on 355 x 238,847 points: hash grid 592 / 649 / 665-670 M
+// lookups/s at two / four / eight bins per gridpoint, nuclide grid 704 M at
+// four and 679 M at eight (on 355 x 11,303 points: 746 M at four, 666 M at
+// eight); four holds up on both grids at half the memory of eight.  Built for the hash and nuclide grids (and
 // by the autotuner when it serves a unionized context from those);
 // XSGB_GUIDE=0 in the environment leaves both out, and so does a device
 // without room for them (the searches then run without them).
@@ -255,18 +259,25 @@ xs_status build_guide(xs_ctx *ctx)
     t.guide = nullptr;
     t.guide_log2 = 0;
     t.binrec = nullptr;
-    int k = 2;
-    while (k < 26 && (1L << (k - 2)) < t.n_gp) k++;
-    if (const char *env = getenv("XSGB_GUIDE_LOG2")) {
-        const int v = atoi(env);
-        if (v >= 1 && v <= 26) k = v;
-    }
-    const size_t bytes = (size_t)t.n_iso * (((size_t)1 << k) + 1) * 4;
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
         cudaGetLastError();
         return XS_OK;
     }
+    // four bins per gridpoint where the device has room for their bin
+    // records (16 GiB kept free), else two
+    int lg = 0;
+    while (lg < 26 && (1L << lg) < t.n_gp) lg++;
+    int k = lg + 2 < 26 ? lg + 2 : 26;
+    auto need = [&](int kk) {
+        return (size_t)t.n_iso * (((size_t)1 << kk) * (kRecordDoubles * 8 + 4) + 4) + ((size_t)16 << 30);
+    };
+    while (k > lg + 1 && need(k) > free_b) k--;
+    if (const char *env = getenv("XSGB_GUIDE_LOG2")) {
+        const int v = atoi(env);
+        if (v >= 1 && v <= 26) k = v;
+    }
+    const size_t bytes = (size_t)t.n_iso * (((size_t)1 << k) + 1) * 4;
     if (free_b < bytes + ((size_t)4 << 30)) return XS_OK;
     void *p = nullptr;
     xs_status s = ctx_alloc(ctx, &p, bytes);
