@@ -341,6 +341,16 @@ def side_measurements(stream, steps, warmup, fp64_peak, peak_gbs):
             "hash_ok": times[-1].hash == 952131,
             "what": "forward macro_xs + dL/dE + dL/dconcs + dL/dxs, device arrays, N(0,1) upstream"}
         del g, d_e, d_c, d_x, macro
+        # the autotuner's choice for this context (xs_autotune: grid type,
+        # guided searches, kernel shapes, block size, in-tile order, on 4M of
+        # its lookups), then the whole batch timed with it
+        t0 = time.perf_counter()
+        best = ctx.autotune()
+        t_tune = time.perf_counter() - t0
+        v, ms, r = time_kernel(ctx, stream, inputs.lookups, steps, warmup, kernel=best["kernel"])
+        out["large_hash_autotuned"] = {"value": v, "unit": UNIT, "ms_per_step": ms,
+                                       "hash_ok": r.hash == 952131, "choice": best,
+                                       "tuning_s": round(t_tune, 1)}
     finally:
         ctx.close()
     # the XL problem on both grids
