@@ -371,10 +371,11 @@ xs_status build_derived_tables(xs_ctx *ctx)
     if (guided) {
         s = build_guide(ctx);
         if (s != XS_OK) return s;
-        // the guided lookups with the in-tile energy sort run best in
-        // tiles of 2,048 (XL: 616 against 518 M lookups/s at 1,024)
-        if (t.guide) ctx->plain_tile = 2048;
     }
+    // with the in-tile energy order (the hash and nuclide grids) the plain
+    // kernel runs best in tiles of 2,048 (XL, guided: 616 against 518 M
+    // lookups/s at 1,024; large hash grid, its own search: 754 against 738 M)
+    if (t.grid_type != XS_UNIONIZED) ctx->plain_tile = 2048;
     if (t.grid_type == XS_UNIONIZED) {
         s = ctx_alloc(ctx, &p, (size_t)t.n_union * 8);
         if (s != XS_OK) return s;
