@@ -157,9 +157,12 @@ xs_status xs_binary_read(const char *path, xs_simdata *out);
 /* ------------------------------------------------------------ device side */
 
 /* Copies one problem to device `device` and builds the device-side derived
- * tables (slope records, search keys, union-grid bins).  Replaces
- * move_simulation_data_to_device (cuda/GridInit.cu:4).  The caller keeps
- * ownership of the host arrays. */
+ * tables (slope records, search keys, union-grid bins; on the nuclide grid,
+ * and on a hash grid whose energy keys exceed L2, an energy-bin guide and
+ * bin records: per nuclide and bin a copy of the interval record the bin's
+ * search starts at, 47.6 GB for the XL problem, built when the device keeps
+ * 16 GiB free beside them).  Replaces move_simulation_data_to_device
+ * (cuda/GridInit.cu:4).  The caller keeps ownership of the host arrays. */
 xs_status xs_ctx_create(const xs_inputs *in, const xs_simdata *sd, int device, xs_ctx **out);
 
 /* Builds the problem directly on the device: the same tables as
