@@ -711,7 +711,13 @@ def main():
     ctx.close()   # frees the device for the side configurations
     if rank == 0 and world == 1 and not args.no_side and not args.gridpoints \
             and args.workload == "large_unionized":
+        side_clocks = ClockSampler(local)
+        side_clocks.start()
+        side_clocks.mark_begin()
         line["side"] = side_measurements(stream, max(3, min(args.steps, 5)), 3, fp64_peak, peak)
+        side_clocks.mark_end()
+        # clocks over the whole side section (set-ups included)
+        line["side"]["clocks"] = side_clocks.stop()
     if rank == 0:
         print(json.dumps(line), flush=True)
     problem.close()
