@@ -427,6 +427,10 @@ def test_guided_search_variants(monkeypatch, name, variant):
             else:
                 rows = fin.all(axis=1)
                 assert rel_err(macro[rows], ref["macro"][rows]) <= REL_TOL
+        # checked runs (every table index bounds-checked) and the batched kernel
+        for kernel in ("plain", "batched"):
+            assert ctx.run_event(kernel=kernel, checked=True).verification == g["verification"]
+            assert ctx.run_event(kernel=kernel).verification == g["verification"]
 
 
 def test_drop_in_seam():
