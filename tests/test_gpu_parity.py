@@ -237,6 +237,37 @@ def test_caller_samples_host_and_device(kernel):
     assert sha(didx.cpu().numpy()) == g["sha256_max_idx"]
 
 
+@pytest.mark.parametrize("name", ["small_unionized", "small_hash"])
+def test_host_sample_pipeline_full_size(name):
+    """The host-sample pipeline over the whole 17,000,000-lookup batch (17
+    chunks on two streams, the plain kernel's overflow passes on the third):
+    the reference's hash and argmax digest in both arithmetics, EXACT macro_xs
+    bit for bit, FAST bit-identical to the device-resident plain run (the
+    overflow pass repeats the tiles' arithmetic lookup for lookup), and the
+    batched kernel's chunks by the same digests."""
+    import torch
+    g = golden_json("full_" + name)
+    ctx = ctx_for(name)
+    n = g["lookups"]
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    E, M = pin((n,), torch.float64), pin((n,), torch.int32)
+    ctx.sample_event(0, n, E, M)
+    macro, idx = pin((n, 5), torch.float64), pin((n,), torch.uint8)
+    r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel="plain", arith="exact")
+    assert r.hash == g["hash"] and r.verification == g["verification"]
+    assert sha(idx) == g["sha256_max_idx"]
+    assert sha(macro) == g["sha256_macro_xs"]
+    _, m_dev, _ = run(ctx, n, kernel="plain", arith="fast")
+    r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel="plain", arith="fast")
+    assert r.verification == g["verification"]
+    assert sha(idx) == g["sha256_max_idx"]
+    assert np.array_equal(macro, m_dev)
+    del m_dev
+    r = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel="batched", arith="fast")
+    assert r.verification == g["verification"]
+    assert sha(idx) == g["sha256_max_idx"]
+
+
 def test_async_runs_then_sync():
     import torch
     g = golden_json("full_tiny_hash")

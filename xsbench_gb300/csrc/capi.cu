@@ -218,10 +218,13 @@ void xs_ctx_destroy(xs_ctx *ctx)
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < xs_ctx::kPipeSlots; i++) {
         if (ctx->pipe_stream[i]) cudaStreamDestroy(ctx->pipe_stream[i]);
         if (ctx->pipe_event[i]) cudaEventDestroy(ctx->pipe_event[i]);
+        if (ctx->ovf_ready[i]) cudaEventDestroy(ctx->ovf_ready[i]);
+        if (ctx->ovf_done[i]) cudaEventDestroy(ctx->ovf_done[i]);
     }
+    if (ctx->ovf_stream) cudaStreamDestroy(ctx->ovf_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -288,9 +291,16 @@ xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    for (int i = 0; i < xs_ctx::kPipeSlots && e == cudaSuccess; i++) {
         e = cudaStreamCreateWithFlags(&ctx->pipe_stream[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->pipe_event[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ovf_ready[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ovf_done[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) {
+        int least = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->ovf_stream, cudaStreamNonBlocking, greatest);
     }
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_result, 64);
     if (e != cudaSuccess) {
@@ -404,6 +414,8 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
     if (const char *env = getenv("XSGB_STAGE_ROWS")) ctx->stage_rows = atoi(env) != 0 ? 1 : 0;
     if (const char *env = getenv("XSGB_TILE_SORT")) ctx->tile_sort = atoi(env) != 0 ? 1 : 0;
     if (const char *env = getenv("XSGB_OVERFLOW")) ctx->overflow = atoi(env) != 0 ? 1 : 0;
+    if (const char *env = getenv("XSGB_PIPE_SLOTS")) ctx->pipe_slots = std::min(std::max(atoi(env), 2), xs_ctx::kPipeSlots);
+    if (const char *env = getenv("XSGB_PIPE_CHUNK")) ctx->pipe_chunk = atol(env);
     if (const char *env = getenv("XSGB_BATCHED_FUEL_LANES")) {
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->batched_fuel_lanes = v;
@@ -587,28 +599,66 @@ xs_status xs_run_event(xs_ctx *ctx, const xs_run_opts *opts, double *macro_xs_ou
     return run_once(ctx, o, SampleInput{}, macro_xs_out, max_idx_out, result);
 }
 
-// Host-resident samples: chunks alternate between two streams, so the copy
-// of one chunk overlaps the lookups of the other.
+// Chunk sizes of the host-sample pipeline: whole chunks in the middle and a
+// ramp of chunk/8, chunk/4, chunk/2 at each end, so that the first chunk's
+// copy in and the last chunk's copy out, which no other chunk's lookups
+// overlap, are short (large problem, 2M-lookup chunks: the last chunk's
+// macro_xs alone took 0.43 ms of a 19 ms run to come back).
+static std::vector<long> pipeline_chunks(long n, long chunk, int tile)
+{
+    std::vector<long> v;
+    const long ramp[3] = {chunk / 8, chunk / 4, chunk / 2};
+    const long ends = 2 * (ramp[0] + ramp[1] + ramp[2]);
+    if (n <= ends + chunk || ramp[0] < tile) {
+        for (long c0 = 0; c0 < n; c0 += chunk) v.push_back(std::min(chunk, n - c0));
+        return v;
+    }
+    for (long r : ramp) v.push_back(r);
+    const long mid = n - ends;
+    const long k = (mid + chunk - 1) / chunk;
+    const long each = std::min(chunk, ((mid + k - 1) / k + tile - 1) / tile * tile);  // whole tiles
+    for (long left = mid; left > 0; left -= each) v.push_back(std::min(each, left));
+    for (int i = 2; i >= 0; i--) v.push_back(ramp[i]);
+    return v;
+}
+
+// Host-resident samples: chunks rotate over the pipeline's streams (one
+// buffer set each), so the copies of some chunks overlap the lookups of
+// others.
 static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *energy,
                                const int *mat, long n, double *macro_out, unsigned char *idx_out,
                                xs_run_result *result)
 {
-    const long chunk = o.tile_lookups > 0 && o.kernel == XS_KERNEL_PLAIN ? std::max<long>(1L << 20, o.tile_lookups) : (1L << 21);
+    // whole chunks of 2^21 lookups (plain) or 2^22 (batched: each chunk is
+    // sorted on its own, and its persistent launch ends in a tail); swept end
+    // to end on the large problem, four slots: plain 2^20 / 2^21 / 2^22 =
+    // 898 / 905 / 898 M lookups/s, batched 2^21 / 2^22 / 2^23 = 920 / 926 / 850 M
+    const long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
+    const long chunk = std::max<long>(ctx->pipe_chunk > 0 ? ctx->pipe_chunk : whole, o.tile_lookups);
     const size_t per = 8 + 4 + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
     const size_t io_bytes = ((size_t)chunk * per + 1023) & ~(size_t)255;
-    // No overflow pass per chunk: each chunk's partial groups run in their
-    // tiles (the same arithmetic per lookup); a persistent overflow launch per
-    // chunk held the GPU between the two streams' tiles (measured end to end:
-    // 0.77 G lookups/s with it, 0.86 G without).
+    // Plain kernel: each chunk's partial 32-lookup groups go to its own
+    // overflow queues, and the chunk's overflow pass runs on the
+    // high-priority stream, so its blocks are dispatched as soon as the
+    // chunk's tiles end instead of after the other streams' pending tiles
+    // (on the tiles' own stream the pass waited behind them and held up the
+    // next chunk: 0.77 G lookups/s end to end, against 0.86 G with the
+    // partial groups padded in their tiles).  A chunk's buffers are reused
+    // by the chunk `slots` places later, which waits for its overflow pass
+    // and copy out: with two slots that chain stalled the 1M-lookup chunks
+    // (large hash grid, end to end: 665 M lookups/s with two slots of 1M,
+    // 723 M with three of 2M, 746 M with four of 2M).
+    const bool ovf = o.kernel == XS_KERNEL_PLAIN && use_overflow(ctx, chunk, o.tile_lookups);
+    const size_t ovf_bytes = ovf ? ((plain_scratch_bytes(chunk, o.tile_lookups) + 255) & ~(size_t)255) : 0;
     // batched: each stream has its own sort buffers, so the two streams overlap
     const bool batched = o.kernel == XS_KERNEL_BATCHED;
     int nb_log2 = 0;
     while ((1 << nb_log2) < o.energy_buckets) nb_log2++;
     if (batched && ((1 << nb_log2) != o.energy_buckets || o.energy_buckets > 65536))
         return fail(XS_ERR_INVALID_ARGUMENT, "energy_buckets %d must be a power of two <= 65536", o.energy_buckets);
-    const size_t slot = io_bytes +
+    const size_t slot = io_bytes + ovf_bytes +
                         (batched ? ((batched_scratch_bytes(chunk, o.energy_buckets) + 255) & ~(size_t)255) : 0);
-    const size_t need = 2 * slot;
+    const size_t need = (size_t)ctx->pipe_slots * slot;
     if (ctx->pipe_bytes < need) {
         if (ctx->pipe_buf) {
             cudaFree(ctx->pipe_buf);
@@ -630,12 +680,15 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
     XS_CUDA(cudaMemsetAsync(ctx->s.verification, 0, 8, main));
     XS_CUDA(cudaMemsetAsync(ctx->s.error, 0, 16, main));
     XS_CUDA(cudaEventRecord(ctx->ev0, main));
-    for (int i = 0; i < 2; i++) XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[i], ctx->ev0, 0));
+    const int S = ctx->pipe_slots;
+    for (int i = 0; i < S; i++) XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[i], ctx->ev0, 0));
     int launches = 0;
-    for (long c0 = 0, k = 0; c0 < n; c0 += chunk, k++) {
-        const int w = (int)(k & 1);
+    const std::vector<long> sizes = pipeline_chunks(n, chunk, o.tile_lookups);
+    long c0 = 0;
+    for (size_t k = 0; k < sizes.size(); c0 += sizes[k], k++) {
+        const int w = (int)(k % S);
         cudaStream_t st = ctx->pipe_stream[w];
-        const long m = std::min(chunk, n - c0);
+        const long m = sizes[k];
         char *b = (char *)ctx->pipe_buf + (size_t)w * slot;
         double *dE = (double *)b;
         int *dM = (int *)(b + (size_t)chunk * 8);
@@ -651,8 +704,11 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         out.max_idx = dIdx;
         xs_status s;
         if (o.kernel == XS_KERNEL_PLAIN) {
+            PlainScratch ps;
+            OverflowStream os{ctx->ovf_stream, ctx->ovf_ready[w], ctx->ovf_done[w]};
+            if (ovf) ps = carve_plain_scratch(b + io_bytes, m, o.tile_lookups);
             s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, o.block_threads, in,
-                             out, nullptr, &launches);
+                             out, ovf ? &ps : nullptr, &launches, ovf ? &os : nullptr);
         } else {
             BatchedScratch bs = carve_batched_scratch(b + io_bytes, chunk, nb_log2);
             bs.verification = ctx->s.verification;
@@ -664,7 +720,7 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));
         if (idx_out) XS_CUDA(cudaMemcpyAsync(idx_out + c0, dIdx, (size_t)m, cudaMemcpyDeviceToHost, st));
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < S; i++) {
         XS_CUDA(cudaEventRecord(ctx->pipe_event[i], ctx->pipe_stream[i]));
         XS_CUDA(cudaStreamWaitEvent(main, ctx->pipe_event[i], 0));
     }

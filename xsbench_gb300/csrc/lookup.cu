@@ -240,7 +240,8 @@ int list_blocks(const xs_ctx *ctx, int block)
 
 xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                        long count, int tile, int block, const SampleInput &in,
-                       const Outputs &out, const PlainScratch *ps, int *launches)
+                       const Outputs &out, const PlainScratch *ps, int *launches,
+                       const OverflowStream *os)
 {
     if (block == 0) {
         block = ctx->plain_block;
@@ -277,6 +278,12 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
     XS_CUDA(plain_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, in.energy != nullptr, a));
     if (launches) *launches += 1;
     if (ps) {
+        cudaStream_t tiles = st;
+        if (os) {
+            XS_CUDA(cudaEventRecord(os->ready, tiles));
+            XS_CUDA(cudaStreamWaitEvent(os->st, os->ready, 0));
+            st = os->st;
+        }
         k_overflow_seg<<<1, 32, 0, st>>>(ps->cnt, ps->cap, ps->seg_v, ps->base);
         XS_CUDA(cudaGetLastError());
         ListArgs l;
@@ -296,6 +303,10 @@ xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, lon
         l.block = ctx->batched_block;
         XS_CUDA(list_fn(ctx->t.grid_type)(ctx->t, st, arith, checked, list_blocks(ctx, l.block), l));
         if (launches) *launches += 2;
+        if (os) {
+            XS_CUDA(cudaEventRecord(os->done, st));
+            XS_CUDA(cudaStreamWaitEvent(tiles, os->done, 0));
+        }
     }
     return XS_OK;
 }

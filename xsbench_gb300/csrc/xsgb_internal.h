@@ -135,9 +135,16 @@ struct xs_ctx {
     void *h_result = nullptr;                 // pinned: verification + error words
     cudaStream_t last_stream = nullptr;       // stream of the last (async) run
     int last_launches = 0;
-    // host-sample pipeline: two streams, two buffer sets
-    cudaStream_t pipe_stream[2] = {nullptr, nullptr};
-    cudaEvent_t pipe_event[2] = {nullptr, nullptr};
+    // host-sample pipeline: `pipe_slots` streams with a buffer set each, and
+    // the plain kernel's overflow passes on one more, high-priority stream
+    static constexpr int kPipeSlots = 4;
+    cudaStream_t pipe_stream[kPipeSlots] = {};
+    cudaEvent_t pipe_event[kPipeSlots] = {};
+    cudaStream_t ovf_stream = nullptr;
+    cudaEvent_t ovf_ready[kPipeSlots] = {};
+    cudaEvent_t ovf_done[kPipeSlots] = {};
+    int pipe_slots = 4;                       // buffer sets (and streams) in use
+    long pipe_chunk = 0;                      // lookups per whole chunk (0: by kernel)
     void *pipe_buf = nullptr;
     size_t pipe_bytes = 0;
     // grids the autotuner may switch to (owned through `allocations`)
@@ -202,12 +209,21 @@ struct PlainScratch {
 };
 size_t plain_scratch_bytes(long count, int tile);
 PlainScratch carve_plain_scratch(void *buf, long count, int tile);
+// Where the overflow pass runs when it is not on the tiles' stream: `st` (a
+// high-priority stream, so the pass's blocks are dispatched ahead of another
+// stream's pending tiles), `ready` recorded after the tiles, `done` after the
+// pass (the tiles' stream waits on it).
+struct OverflowStream {
+    cudaStream_t st;
+    cudaEvent_t ready, done;
+};
 // ps == null: each block runs the partial chunks of its tile with idle lanes.
 // block: threads per block (128, 256 or 512; 0 = the context's, halved while
-// above the tile).
+// above the tile).  os == null: the overflow pass follows the tiles on `st`.
 xs_status launch_plain(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                        long count, int tile, int block, const SampleInput &in,
-                       const Outputs &out, const PlainScratch *ps, int *launches);
+                       const Outputs &out, const PlainScratch *ps, int *launches,
+                       const OverflowStream *os = nullptr);
 xs_status launch_batched(xs_ctx *ctx, cudaStream_t st, int arith, int checked, long first,
                          long count, int block, int buckets, const SampleInput &in,
                          const Outputs &out, int *launches);
