@@ -225,6 +225,7 @@ void xs_ctx_destroy(xs_ctx *ctx)
         if (ctx->ovf_done[i]) cudaEventDestroy(ctx->ovf_done[i]);
     }
     if (ctx->ovf_stream) cudaStreamDestroy(ctx->ovf_stream);
+    if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -297,6 +298,7 @@ xs_status ctx_open(const xs_inputs *in, int device, xs_ctx **out)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ovf_ready[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ovf_done[i], cudaEventDisableTiming);
     }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_event, cudaEventDisableTiming);
     if (e == cudaSuccess) {
         int least = 0, greatest = 0;
         e = cudaDeviceGetStreamPriorityRange(&least, &greatest);

@@ -585,13 +585,14 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
 {
     const int nl = ctx->inputs.lookups;
     // A step is one batch of `count` lookups (500,000 at the default size),
-    // too few to fill the GPU, so each step lasts about as long as its
-    // longest fuel lookups: FAST (fuel over 4 lanes) wants small tiles,
-    // EXACT (fuel on one lane, 321 nuclides in order) large ones; and the
-    // overflow pass would add one more such chain per step (measured, large
-    // problem: FAST 609 M lookups/s at 256 with no overflow pass, EXACT 172 M
-    // at 2,048 against 115-130 M with the pass)
-    if (tile <= 0) tile = arith == XS_ARITH_EXACT ? 2048 : 256;
+    // too few to fill the GPU, so a step lasts about as long as its longest
+    // fuel lookups; the overflow pass would add one more such chain per step
+    // (EXACT 172 M lookups/s against 115-130 M with the pass, one group).
+    // Tiles measured with four groups (large problem, unionized / hash /
+    // nuclide grid): FAST 256: 762 / 610 / 591 M, 512: 824 / 619 / 648 M,
+    // 1,024: 725 / 594 / 565 M; EXACT 1,024: 219 / 210 / 202 M, 2,048:
+    // 183 / 169 / 164 M.
+    if (tile <= 0) tile = arith == XS_ARITH_EXACT ? 1024 : 512;
     const size_t need = (size_t)count * (8 + 8 + 4 + 40) + 4096;
     if (ctx->s.hist_bytes < need) {
         if (ctx->s.hist_buf) {
@@ -618,18 +619,46 @@ xs_status launch_history_stepped(xs_ctx *ctx, cudaStream_t st, int arith, long f
     k_history_init<<<blocks, 256, 0, st>>>(ctx->t, first, count, nl, seed, E, mat);
     XS_CUDA(cudaGetLastError());
     int n = 1;
-    SampleInput in;
-    in.energy = E;
-    in.mat = mat;
-    Outputs out;
-    out.macro = macro;
+    // The particles in up to four contiguous groups, each on a stream of its
+    // own through all its steps: a group's step ends in a tail (its longest
+    // fuel lookups), which the other groups' steps fill.  Particles are
+    // independent, so the groups' steps need no order among themselves.
+    const int groups = count >= 4L * 65536 ? xs_ctx::kPipeSlots : 1;
+    cudaStream_t gs[xs_ctx::kPipeSlots];
+    long lo[xs_ctx::kPipeSlots + 1];
+    for (int g = 0; g <= groups; g++) lo[g] = count * g / groups;
+    if (groups > 1) {
+        XS_CUDA(cudaEventRecord(ctx->fork_event, st));
+        for (int g = 0; g < groups; g++) {
+            gs[g] = ctx->pipe_stream[g];
+            XS_CUDA(cudaStreamWaitEvent(gs[g], ctx->fork_event, 0));
+        }
+    } else {
+        gs[0] = st;
+    }
     for (int step = 0; step < nl; step++) {
-        xs_status s = launch_plain(ctx, st, arith, 0, 0, count, tile, 0, in, out, nullptr, &n);
-        if (s != XS_OK) return s;
-        if (step + 1 < nl) {
-            k_history_advance<<<blocks, 256, 0, st>>>(ctx->t, count, macro, seed, E, mat);
-            XS_CUDA(cudaGetLastError());
-            n++;
+        for (int g = 0; g < groups; g++) {
+            const long m = lo[g + 1] - lo[g];
+            SampleInput in;
+            in.energy = E + lo[g];
+            in.mat = mat + lo[g];
+            Outputs out;
+            out.macro = macro + lo[g] * 5;
+            xs_status s = launch_plain(ctx, gs[g], arith, 0, 0, m, tile, 0, in, out, nullptr, &n);
+            if (s != XS_OK) return s;
+            if (step + 1 < nl) {
+                const unsigned b = (unsigned)std::min<long>((m + 255) / 256, (long)ctx->sm_count * 16);
+                k_history_advance<<<b, 256, 0, gs[g]>>>(ctx->t, m, macro + lo[g] * 5, seed + lo[g],
+                                                        E + lo[g], mat + lo[g]);
+                XS_CUDA(cudaGetLastError());
+                n++;
+            }
+        }
+    }
+    if (groups > 1) {
+        for (int g = 0; g < groups; g++) {
+            XS_CUDA(cudaEventRecord(ctx->pipe_event[g], gs[g]));
+            XS_CUDA(cudaStreamWaitEvent(st, ctx->pipe_event[g], 0));
         }
     }
     if (launches) *launches += n;

@@ -143,6 +143,7 @@ struct xs_ctx {
     cudaStream_t ovf_stream = nullptr;
     cudaEvent_t ovf_ready[kPipeSlots] = {};
     cudaEvent_t ovf_done[kPipeSlots] = {};
+    cudaEvent_t fork_event = nullptr;         // stepped history: the groups' start
     int pipe_slots = 4;                       // buffer sets (and streams) in use
     long pipe_chunk = 0;                      // lookups per whole chunk (0: by kernel)
     void *pipe_buf = nullptr;
