@@ -277,6 +277,20 @@ def side_measurements(stream, steps, warmup, fp64_peak, peak_gbs):
     import torch
     import xsbench_gb300 as X
     out = {}
+    # the practical DRAM ceiling of the plain kernels' access pattern: whole
+    # 128-byte lines gathered at random, a warp's 32 lanes inside one window
+    # (xsbench_gb300/_lib/xsgb_gather_ceiling, 8 GB buffer, about 2 s)
+    ceiling = None
+    probe = os.path.join(ROOT, "xsbench_gb300", "_lib", "xsgb_gather_ceiling")
+    if os.path.exists(probe):
+        try:
+            p = subprocess.run([probe, "33"], capture_output=True, text=True, timeout=120)
+            g = json.loads(p.stdout.strip().splitlines()[-1])
+            if p.returncode == 0 and "windows" in g:
+                out["gather_ceiling"] = g
+                ceiling = max(w["gbs"] for w in g["windows"] if w["window_bytes"] == 1 << 24)
+        except (subprocess.SubprocessError, ValueError, IndexError) as e:
+            out["gather_ceiling"] = {"unavailable": str(e)[:200]}
 
     def plain_key(wl_name, wl, ctx, inputs, nn):
         exp = expected_hash(wl)
@@ -294,6 +308,8 @@ def side_measurements(stream, steps, warmup, fp64_peak, peak_gbs):
         if dram:
             rec["dram"] = {"bytes_per_lookup": dram, "achieved_gbs": v * dram / 1e9,
                            "frac": v * dram / 1e9 / peak_gbs, "source": src}
+            if ceiling:
+                rec["dram"]["frac_of_gather_ceiling"] = v * dram / 1e9 / ceiling
         return rec
 
     def batched_key(wl_name, wl, ctx, inputs, nn, ops_per_nuclide=11):

@@ -1,6 +1,7 @@
 """In-tree build of the GB300 library and its C driver.
 
-    python -m xsbench_gb300.build            # -> xsbench_gb300/_lib/libxsgb.so, xsgb
+    python -m xsbench_gb300.build            # -> xsbench_gb300/_lib/libxsgb.so, xsgb,
+                                             #    xsgb_gather_ceiling
     python -m xsbench_gb300.build --ptxas-v  # also print registers / spills
 
 Every CUDA translation unit is compiled for sm_103a only
@@ -23,6 +24,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libxsgb.so")
 EXE_PATH = os.path.join(LIB_DIR, "xsgb")
+PROBE_PATH = os.path.join(LIB_DIR, "xsgb_gather_ceiling")
 
 CU_SOURCES = ["capi.cu", "setup_host.cu", "tables.cu", "lookup.cu", "lookup_unionized.cu",
               "lookup_nuclide.cu", "lookup_hash.cu", "static_scratch.cu", "adjoint.cu", "tune.cu",
@@ -61,6 +63,10 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> 
     flags += os.environ.get("XSGB_NVCC_FLAGS", "").split()
     jobs = []
     objs = []
+    # the gather-ceiling probe: a standalone binary, built beside the library
+    probe = os.path.join(CSRC, "gather_ceiling.cu")
+    if force or _stale(PROBE_PATH, [probe]):
+        jobs.append([nv, "-O3", "-std=c++17", *GENCODE, "-o", PROBE_PATH, probe])
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
