@@ -94,3 +94,13 @@ def test_driver_binary_built():
     assert os.access(B.EXE_PATH, os.X_OK)
     p = subprocess.run([B.EXE_PATH, "-q"], capture_output=True, text=True)
     assert p.returncode == 2 and "invalid argument" in p.stderr
+
+
+def test_gather_ceiling_probe_is_built_and_checks_its_argument():
+    """build() leaves the gather-ceiling probe beside the library; it is an
+    sm_103a binary, and it refuses a buffer size outside [2^28, 2^37] before
+    touching any device."""
+    from xsbench_gb300 import build as B
+    assert os.path.exists(B.PROBE_PATH) and os.access(B.PROBE_PATH, os.X_OK)
+    p = subprocess.run([B.PROBE_PATH, "40"], capture_output=True, text=True, timeout=60)
+    assert p.returncode == 2 and "buffer_log2" in p.stdout
