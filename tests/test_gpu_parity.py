@@ -237,10 +237,11 @@ def test_caller_samples_host_and_device(kernel):
     assert sha(didx.cpu().numpy()) == g["sha256_max_idx"]
 
 
-@pytest.mark.parametrize("name", ["small_unionized", "small_hash"])
+@pytest.mark.parametrize("name", ["small_unionized", "small_hash", "large_unionized"])
 def test_host_sample_pipeline_full_size(name):
-    """The host-sample pipeline over the whole 17,000,000-lookup batch (17
-    chunks on two streams, the plain kernel's overflow passes on the third):
+    """The host-sample pipeline over the whole 17,000,000-lookup batch (13
+    chunks on four streams, the plain kernel's overflow passes on a fifth;
+    the large problem is the bench's end-to-end configuration):
     the reference's hash and argmax digest in both arithmetics, EXACT macro_xs
     bit for bit, FAST bit-identical to the device-resident plain run (the
     overflow pass repeats the tiles' arithmetic lookup for lookup), and the
