@@ -269,6 +269,41 @@ def test_host_sample_pipeline_full_size(name):
     assert sha(idx) == g["sha256_max_idx"]
 
 
+@pytest.mark.parametrize("n", [1, 31, 262145, 2097153, 5767169, 11534337])
+def test_host_pipeline_chunk_edges(n):
+    """The host-sample pipeline at batch sizes around its chunk schedule
+    (whole chunks of 2^21 lookups plain, 2^22 batched; ramps of 1/8, 1/4, 1/2
+    chunk at both ends above 2.75 chunks): one lookup, under one warp, a ramp
+    chunk plus one, a plain chunk plus one, the plain ramp with ragged middle
+    chunks, and the batched ramp.  Against the same samples
+    from device arrays (one launch): EXACT bit for bit, the batched kernel bit
+    for bit in both arithmetics, the plain kernel's FAST within REL_TOL (a short
+    device-resident batch runs a material's partial warp of lookups split over
+    lanes, the pipeline's chunks send it to the overflow pass), the argmax
+    vector and the verification sum identical."""
+    import torch
+    ctx = ctx_for("tiny_hash")
+    E, M = np.empty(n), np.empty(n, np.int32)
+    ctx.sample_event(0, n, E, M)
+    dE, dM = torch.from_numpy(E).cuda(), torch.from_numpy(M).cuda()
+    for kernel in ("plain", "batched"):
+        for arith in ("exact", "fast"):
+            dmacro = torch.empty((n, 5), dtype=torch.float64, device="cuda")
+            didx = torch.empty(n, dtype=torch.uint8, device="cuda")
+            rd = ctx.lookup_samples(dE, dM, macro_out=dmacro, max_idx_out=didx, kernel=kernel,
+                                    arith=arith)
+            macro, idx = np.empty((n, 5)), np.empty(n, np.uint8)
+            rh = ctx.lookup_samples(E, M, macro_out=macro, max_idx_out=idx, kernel=kernel,
+                                    arith=arith)
+            key = (kernel, arith)
+            assert rh.verification == rd.verification, key
+            assert np.array_equal(idx, didx.cpu().numpy()), key
+            if kernel == "plain" and arith == "fast":
+                assert rel_err(macro, dmacro.cpu().numpy()) <= REL_TOL, key
+            else:
+                assert np.array_equal(macro, dmacro.cpu().numpy()), key
+
+
 def test_async_runs_then_sync():
     import torch
     g = golden_json("full_tiny_hash")
