@@ -219,7 +219,10 @@ xs_status xs_ctx_sync(xs_ctx *ctx, xs_run_result *result);
  * of optimisation 1 (openmp-threading/Simulation.c:735-750,
  * cuda/Simulation.cu:441) with the samples owned by the caller.  Arrays may be
  * host or device memory; host arrays are streamed through the device in
- * overlapped chunks.  Materials outside 0..11 give XS_ERR_DATA. */
+ * overlapped chunks (their copies overlap the lookups when the host arrays
+ * are page-locked, cudaHostAlloc / cudaHostRegister; pageable arrays work,
+ * but the driver stages their copies and they serialise).  Materials outside
+ * 0..11 give XS_ERR_DATA. */
 xs_status xs_lookup_samples(xs_ctx *ctx, const xs_run_opts *opts, const double *energy,
                             const int *mat, long n, double *macro_xs_out,
                             unsigned char *max_idx_out, xs_run_result *result);
