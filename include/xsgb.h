@@ -200,7 +200,10 @@ void xs_run_opts_init(xs_run_opts *opts);
 /* Event-based lookups [first, first+count) with in-kernel LCG sampling: the
  * drop-in for run_event_based_simulation (openmp-threading/Simulation.c:15;
  * cuda/Simulation.cu:15 and :1024).  macro_xs_out (count*5 doubles) and
- * max_idx_out (count bytes, argmax 0..4) may be NULL. */
+ * max_idx_out (count bytes, argmax 0..4) may be NULL, device or host memory;
+ * host outputs (every non-NULL one) are filled chunk by chunk, each chunk's
+ * copy overlapping the next chunks' lookups (page-locked host memory lets
+ * the copies overlap); device_ms then covers the copies too. */
 xs_status xs_run_event(xs_ctx *ctx, const xs_run_opts *opts, double *macro_xs_out,
                        unsigned char *max_idx_out, xs_run_result *result);
 

@@ -528,6 +528,10 @@ xs_status xs_ctx_sync(xs_ctx *ctx, xs_run_result *result)
     return s;
 }
 
+static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *energy,
+                               const int *mat, long n, double *macro_out, unsigned char *idx_out,
+                               xs_run_result *result);
+
 // Shared by xs_run_event (samples == NULL) and device-resident xs_lookup_samples.
 static xs_status run_once(xs_ctx *ctx, const xs_run_opts &o, const SampleInput &in,
                           double *macro_out, unsigned char *idx_out, xs_run_result *result)
@@ -538,6 +542,10 @@ static xs_status run_once(xs_ctx *ctx, const xs_run_opts &o, const SampleInput &
     const bool host_idx = idx_out && !is_device_pointer(idx_out);
     if (o.async && (host_macro || host_idx))
         return fail(XS_ERR_INVALID_ARGUMENT, "async runs take device (or NULL) output arrays");
+    // the event batch's own samples with every output on the host: chunks
+    // whose copies out overlap the next chunks' lookups
+    if (!in.energy && (host_macro || host_idx) && (!macro_out || host_macro) && (!idx_out || host_idx))
+        return run_pipelined(ctx, o, nullptr, nullptr, n, macro_out, idx_out, result);
     Outputs out;
     out.macro = macro_out;
     out.max_idx = idx_out;
@@ -624,20 +632,23 @@ static std::vector<long> pipeline_chunks(long n, long chunk, int tile)
     return v;
 }
 
-// Host-resident samples: chunks rotate over the pipeline's streams (one
-// buffer set each), so the copies of some chunks overlap the lookups of
-// others.
+// Host-resident samples (energy, mat), or with energy == NULL the event
+// batch's own LCG samples of lookups o.first + i (nothing copied in): chunks
+// rotate over the pipeline's streams (one buffer set each), so the copies of
+// some chunks overlap the lookups of others.
 static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *energy,
                                const int *mat, long n, double *macro_out, unsigned char *idx_out,
                                xs_run_result *result)
 {
+    const bool host_in = energy != nullptr;
     // whole chunks of 2^21 lookups (plain) or 2^22 (batched: each chunk is
     // sorted on its own, and its persistent launch ends in a tail); swept end
     // to end on the large problem, four slots: plain 2^20 / 2^21 / 2^22 =
     // 898 / 905 / 898 M lookups/s, batched 2^21 / 2^22 / 2^23 = 920 / 926 / 850 M
     const long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
     const long chunk = std::max<long>(ctx->pipe_chunk > 0 ? ctx->pipe_chunk : whole, o.tile_lookups);
-    const size_t per = 8 + 4 + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
+    const size_t in_per = host_in ? 12 : 0;
+    const size_t per = in_per + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
     const size_t io_bytes = ((size_t)chunk * per + 1023) & ~(size_t)255;
     // Plain kernel: each chunk's partial 32-lookup groups go to its own
     // overflow queues, and the chunk's overflow pass runs on the
@@ -694,13 +705,17 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
         char *b = (char *)ctx->pipe_buf + (size_t)w * slot;
         double *dE = (double *)b;
         int *dM = (int *)(b + (size_t)chunk * 8);
-        double *dMacro = macro_out ? (double *)(b + (size_t)chunk * 12) : nullptr;
-        unsigned char *dIdx = idx_out ? (unsigned char *)(b + (size_t)chunk * (12 + (macro_out ? 40 : 0))) : nullptr;
-        XS_CUDA(cudaMemcpyAsync(dE, energy + c0, (size_t)m * 8, cudaMemcpyHostToDevice, st));
-        XS_CUDA(cudaMemcpyAsync(dM, mat + c0, (size_t)m * 4, cudaMemcpyHostToDevice, st));
+        double *dMacro = macro_out ? (double *)(b + (size_t)chunk * in_per) : nullptr;
+        unsigned char *dIdx = idx_out ? (unsigned char *)(b + (size_t)chunk * (in_per + (macro_out ? 40 : 0))) : nullptr;
         SampleInput in;
-        in.energy = dE;
-        in.mat = dM;
+        if (host_in) {
+            XS_CUDA(cudaMemcpyAsync(dE, energy + c0, (size_t)m * 8, cudaMemcpyHostToDevice, st));
+            XS_CUDA(cudaMemcpyAsync(dM, mat + c0, (size_t)m * 4, cudaMemcpyHostToDevice, st));
+            in.energy = dE;
+            in.mat = dM;
+        }
+        // lookups sampled in the kernels are numbered from the run's first
+        const long first = host_in ? 0 : o.first + c0;
         Outputs out;
         out.macro = dMacro;
         out.max_idx = dIdx;
@@ -709,14 +724,14 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
             PlainScratch ps;
             OverflowStream os{ctx->ovf_stream, ctx->ovf_ready[w], ctx->ovf_done[w]};
             if (ovf) ps = carve_plain_scratch(b + io_bytes, m, o.tile_lookups);
-            s = launch_plain(ctx, st, o.arith, o.checked, 0, m, o.tile_lookups, o.block_threads, in,
-                             out, ovf ? &ps : nullptr, &launches, ovf ? &os : nullptr);
+            s = launch_plain(ctx, st, o.arith, o.checked, first, m, o.tile_lookups, o.block_threads,
+                             in, out, ovf ? &ps : nullptr, &launches, ovf ? &os : nullptr);
         } else {
             BatchedScratch bs = carve_batched_scratch(b + io_bytes, chunk, nb_log2);
             bs.verification = ctx->s.verification;
             bs.error = ctx->s.error;
-            s = enqueue_batched_buf(ctx, st, o.arith, o.checked, 0, m, nb_log2, o.block_threads, in,
-                                    out, bs, &launches);
+            s = enqueue_batched_buf(ctx, st, o.arith, o.checked, first, m, nb_log2, o.block_threads,
+                                    in, out, bs, &launches);
         }
         if (s != XS_OK) return s;
         if (macro_out) XS_CUDA(cudaMemcpyAsync(macro_out + c0 * 5, dMacro, (size_t)m * 40, cudaMemcpyDeviceToHost, st));
