@@ -645,7 +645,12 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
     // sorted on its own, and its persistent launch ends in a tail); swept end
     // to end on the large problem, four slots: plain 2^20 / 2^21 / 2^22 =
     // 898 / 905 / 898 M lookups/s, batched 2^21 / 2^22 / 2^23 = 920 / 926 / 850 M
-    const long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
+    // A long batch takes whole chunks of about n / 8 (at most 2^24): its
+    // pipeline's ends cost little beside it, and each chunk has a tail (XL,
+    // 100M lookups, end to end: hash grid 619 / 625 / 629 / 631 M lookups/s
+    // with chunks of 2^21 / 2^22 / 2^23 / 2^24).
+    long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
+    while (whole < (1L << 24) && whole * 2 <= n / 8) whole *= 2;
     const long chunk = std::max<long>(ctx->pipe_chunk > 0 ? ctx->pipe_chunk : whole, o.tile_lookups);
     const size_t in_per = host_in ? 12 : 0;
     const size_t per = in_per + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
