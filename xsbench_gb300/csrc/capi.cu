@@ -641,14 +641,14 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
                                xs_run_result *result)
 {
     const bool host_in = energy != nullptr;
-    // whole chunks of 2^21 lookups (plain) or 2^22 (batched: each chunk is
+    // Whole chunks of 2^21 lookups (plain) or 2^22 (batched: each chunk is
     // sorted on its own, and its persistent launch ends in a tail); swept end
     // to end on the large problem, four slots: plain 2^20 / 2^21 / 2^22 =
-    // 898 / 905 / 898 M lookups/s, batched 2^21 / 2^22 / 2^23 = 920 / 926 / 850 M
-    // A long batch takes whole chunks of about n / 8 (at most 2^24): its
-    // pipeline's ends cost little beside it, and each chunk has a tail (XL,
-    // 100M lookups, end to end: hash grid 619 / 625 / 629 / 631 M lookups/s
-    // with chunks of 2^21 / 2^22 / 2^23 / 2^24).
+    // 898 / 905 / 898 M lookups/s, batched 2^21 / 2^22 / 2^23 = 920 / 926 /
+    // 850 M.  A longer batch takes whole chunks of about n / 8 (at most 2^24):
+    // its pipeline's ends cost little beside it, and each chunk has a tail
+    // (XL, 100M lookups: hash grid 619 / 625 / 629 / 631 M lookups/s with
+    // chunks of 2^21 / 2^22 / 2^23 / 2^24).
     long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
     while (whole < (1L << 24) && whole * 2 <= n / 8) whole *= 2;
     const long chunk = std::max<long>(ctx->pipe_chunk > 0 ? ctx->pipe_chunk : whole, o.tile_lookups);
@@ -668,7 +668,7 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
     // 723 M with three of 2M, 746 M with four of 2M).
     const bool ovf = o.kernel == XS_KERNEL_PLAIN && use_overflow(ctx, chunk, o.tile_lookups);
     const size_t ovf_bytes = ovf ? ((plain_scratch_bytes(chunk, o.tile_lookups) + 255) & ~(size_t)255) : 0;
-    // batched: each stream has its own sort buffers, so the two streams overlap
+    // batched: each slot has its own sort buffers, so the streams overlap
     const bool batched = o.kernel == XS_KERNEL_BATCHED;
     int nb_log2 = 0;
     while ((1 << nb_log2) < o.energy_buckets) nb_log2++;
