@@ -389,6 +389,25 @@ def side_measurements(stream, steps, warmup, fp64_peak, peak_gbs):
             out["large_unionized_batched_no_union_table"]["union_table"] = ctx.union_table_bytes > 0
         finally:
             ctx.close()
+        # history mode on the same problem (500,000 particles x 34 lookups,
+        # Simulation.c:116-238): the particles stepped in lockstep as event
+        # batches, and one thread per particle as the reference runs it
+        hin = X.make_inputs(size="large", grid="unionized", method="history")
+        ctx = X.Context(hin)
+        try:
+            n = hin.particles * hin.lookups
+            hist = {}
+            for kernel, reps in (("batched", 5), ("plain", 2)):
+                ctx.run_history(kernel=kernel)
+                runs = [ctx.run_history(kernel=kernel) for _ in range(reps)]
+                t = statistics.median(r.device_ms for r in runs) / 1e3
+                hist[kernel] = {"value": n / t, "unit": UNIT, "ms_per_run": t * 1e3,
+                                "hash": runs[-1].hash, "hash_ok": runs[-1].hash == 954318}
+            out["large_unionized_history"] = {
+                "particles": hin.particles, "lookups_per_particle": hin.lookups,
+                "stepped": hist["batched"], "per_particle": hist["plain"]}
+        finally:
+            ctx.close()
     finally:
         del os.environ["XSGB_UNION_TABLE"]
     out["reference_cuda"] = reference_cuda_kernels()
