@@ -418,6 +418,7 @@ xs_status install_materials(xs_ctx *ctx, const xs_inputs *in, const xs_simdata *
     if (const char *env = getenv("XSGB_OVERFLOW")) ctx->overflow = atoi(env) != 0 ? 1 : 0;
     if (const char *env = getenv("XSGB_PIPE_SLOTS")) ctx->pipe_slots = std::min(std::max(atoi(env), 2), xs_ctx::kPipeSlots);
     if (const char *env = getenv("XSGB_PIPE_CHUNK")) ctx->pipe_chunk = atol(env);
+    if (const char *env = getenv("XSGB_HIST_GROUPS")) ctx->hist_groups = std::min(std::max(atoi(env), 1), xs_ctx::kPipeSlots);
     if (const char *env = getenv("XSGB_BATCHED_FUEL_LANES")) {
         const int v = atoi(env);
         if (v == 1 || v == 2 || v == 4) ctx->batched_fuel_lanes = v;

@@ -137,7 +137,7 @@ struct xs_ctx {
     int last_launches = 0;
     // host-sample pipeline: `pipe_slots` streams with a buffer set each, and
     // the plain kernel's overflow passes on one more, high-priority stream
-    static constexpr int kPipeSlots = 4;
+    static constexpr int kPipeSlots = 8;
     cudaStream_t pipe_stream[kPipeSlots] = {};
     cudaEvent_t pipe_event[kPipeSlots] = {};
     cudaStream_t ovf_stream = nullptr;
@@ -145,6 +145,7 @@ struct xs_ctx {
     cudaEvent_t ovf_done[kPipeSlots] = {};
     cudaEvent_t fork_event = nullptr;         // stepped history: the groups' start
     int pipe_slots = 4;                       // buffer sets (and streams) in use
+    int hist_groups = 8;                      // stepped history: particle groups (streams)
     long pipe_chunk = 0;                      // lookups per whole chunk (0: by kernel)
     void *pipe_buf = nullptr;
     size_t pipe_bytes = 0;
