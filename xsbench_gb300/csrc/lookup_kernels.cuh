@@ -114,6 +114,19 @@ __device__ __forceinline__ bool sample_at(const Tables &t, const double *in_E, c
     }
 }
 
+// A lookup's outputs, written with the streaming (evict-first) store: they
+// are not read again by the kernel, and the sorted lists of the batched form
+// write them at scattered addresses.
+__device__ __forceinline__ void store_result(double *out_macro, unsigned char *out_idx, long o,
+                                             const double macro[5], int arg)
+{
+    if (out_macro) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) __stcs(&out_macro[o * 5 + k], macro[k]);
+    }
+    if (out_idx) __stcs(reinterpret_cast<signed char *>(&out_idx[o]), (signed char)arg);
+}
+
 // One lookup of the event batch: macro_xs, argmax, outputs.
 template <int GRID, int ARITH, bool CHECKED, bool TABLE, bool SROW = false>
 __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, int m, long o,
@@ -123,11 +136,7 @@ __device__ __forceinline__ unsigned lookup_and_store(const Tables &t, double E, 
     double macro[5];
     macro_xs<GRID, ARITH, CHECKED, false, TABLE, SROW>(t, E, m, macro, err, nullptr, 0, 1, sr);
     const int arg = argmax5(macro);
-    if (out_macro) {
-#pragma unroll
-        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
-    }
-    if (out_idx) out_idx[o] = (unsigned char)arg;
+    store_result(out_macro, out_idx, o, macro, arg);
     return (unsigned)(arg + 1);
 }
 
@@ -154,11 +163,7 @@ __device__ __forceinline__ unsigned split_lookup_and_store(const Tables &t, bool
     }
     if (!live || q != 0) return 0;
     const int arg = argmax5(macro);
-    if (out_macro) {
-#pragma unroll
-        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
-    }
-    if (out_idx) out_idx[o] = (unsigned char)arg;
+    store_result(out_macro, out_idx, o, macro, arg);
     return (unsigned)(arg + 1);
 }
 
@@ -192,11 +197,7 @@ __device__ __forceinline__ unsigned nuclide_warp_lookup_and_store(const Tables &
     macro_xs_nuclide_warp<ARITH, CHECKED, GRID == XS_HASH>(t, E, m, live, qmin, qmax, macro, err);
     if (!live) return 0;
     const int arg = argmax5(macro);
-    if (out_macro) {
-#pragma unroll
-        for (int k = 0; k < 5; k++) out_macro[o * 5 + k] = macro[k];
-    }
-    if (out_idx) out_idx[o] = (unsigned char)arg;
+    store_result(out_macro, out_idx, o, macro, arg);
     return (unsigned)(arg + 1);
 }
 
