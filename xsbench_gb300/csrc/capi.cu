@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "pipeline_chunks.h"
 
 namespace xsgb {
 
@@ -610,28 +611,6 @@ xs_status xs_run_event(xs_ctx *ctx, const xs_run_opts *opts, double *macro_xs_ou
     return run_once(ctx, o, SampleInput{}, macro_xs_out, max_idx_out, result);
 }
 
-// Chunk sizes of the host-sample pipeline: whole chunks in the middle and a
-// ramp of chunk/8, chunk/4, chunk/2 at each end, so that the first chunk's
-// copy in and the last chunk's copy out, which no other chunk's lookups
-// overlap, are short (large problem, 2M-lookup chunks: the last chunk's
-// macro_xs alone took 0.43 ms of a 19 ms run to come back).
-static std::vector<long> pipeline_chunks(long n, long chunk, int tile)
-{
-    std::vector<long> v;
-    const long ramp[3] = {chunk / 8, chunk / 4, chunk / 2};
-    const long ends = 2 * (ramp[0] + ramp[1] + ramp[2]);
-    if (n <= ends + chunk || ramp[0] < tile) {
-        for (long c0 = 0; c0 < n; c0 += chunk) v.push_back(std::min(chunk, n - c0));
-        return v;
-    }
-    for (long r : ramp) v.push_back(r);
-    const long mid = n - ends;
-    const long k = (mid + chunk - 1) / chunk;
-    const long each = std::min(chunk, ((mid + k - 1) / k + tile - 1) / tile * tile);  // whole tiles
-    for (long left = mid; left > 0; left -= each) v.push_back(std::min(each, left));
-    for (int i = 2; i >= 0; i--) v.push_back(ramp[i]);
-    return v;
-}
 
 // Host-resident samples (energy, mat), or with energy == NULL the event
 // batch's own LCG samples of lookups o.first + i (nothing copied in): chunks
@@ -650,9 +629,9 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
     // its pipeline's ends cost little beside it, and each chunk has a tail
     // (XL, 100M lookups: hash grid 619 / 625 / 629 / 631 M lookups/s with
     // chunks of 2^21 / 2^22 / 2^23 / 2^24).
-    long whole = o.kernel == XS_KERNEL_BATCHED ? (1L << 22) : (1L << 21);
-    while (whole < (1L << 24) && whole * 2 <= n / 8) whole *= 2;
-    const long chunk = std::max<long>(ctx->pipe_chunk > 0 ? ctx->pipe_chunk : whole, o.tile_lookups);
+    const long chunk = ctx->pipe_chunk > 0 ? std::max<long>(ctx->pipe_chunk, o.tile_lookups)
+                                           : xsgb_pipeline_whole(n, o.kernel == XS_KERNEL_BATCHED,
+                                                                 o.tile_lookups);
     const size_t in_per = host_in ? 12 : 0;
     const size_t per = in_per + (macro_out ? 40 : 0) + (idx_out ? 1 : 0);
     const size_t io_bytes = ((size_t)chunk * per + 1023) & ~(size_t)255;
@@ -702,7 +681,8 @@ static xs_status run_pipelined(xs_ctx *ctx, const xs_run_opts &o, const double *
     const int S = ctx->pipe_slots;
     for (int i = 0; i < S; i++) XS_CUDA(cudaStreamWaitEvent(ctx->pipe_stream[i], ctx->ev0, 0));
     int launches = 0;
-    const std::vector<long> sizes = pipeline_chunks(n, chunk, o.tile_lookups);
+    std::vector<long> sizes((size_t)xsgb_pipeline_chunks(n, chunk, o.tile_lookups, nullptr, 0));
+    xsgb_pipeline_chunks(n, chunk, o.tile_lookups, sizes.data(), (long)sizes.size());
     long c0 = 0;
     for (size_t k = 0; k < sizes.size(); c0 += sizes[k], k++) {
         const int w = (int)(k % S);
