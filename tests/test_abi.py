@@ -104,3 +104,49 @@ def test_gather_ceiling_probe_is_built_and_checks_its_argument():
     assert os.path.exists(B.PROBE_PATH) and os.access(B.PROBE_PATH, os.X_OK)
     p = subprocess.run([B.PROBE_PATH, "40"], capture_output=True, text=True, timeout=60)
     assert p.returncode == 2 and "buffer_log2" in p.stdout
+
+
+DROP_IN = r"""
+#include "XSbench_header.h"
+#include "xsgb.h"
+/* the binding of the reference's Main.c:82-83 (event-based, kernel 0) */
+unsigned long long drop_in(Inputs in, SimulationData SD, int mype, int *status)
+{
+    unsigned long long verification = 0;
+    xs_status st = xs_run_event_based_simulation(*(xs_inputs *)&in, *(xs_simdata *)&SD, mype,
+                                                 &verification);
+    *status = (int)st;
+    return verification;
+}
+int main(void)
+{
+    Inputs in;
+    SimulationData SD;
+    memset(&in, 0, sizeof in);
+    memset(&SD, 0, sizeof SD);
+    int st = 0;
+    drop_in(in, SD, 0, &st);
+    printf("%d %s\n", st, xs_status_str((xs_status)st));
+    return 0;
+}
+"""
+
+
+def test_drop_in_binding_compiles_with_the_reference_header(tmp_path):
+    """The call a maintainer adds to the reference's Main.c compiles in one
+    translation unit with the reference's own XSbench_header.h (no clashing
+    names, struct casts as the integration notes show) and links against the
+    library; an empty problem is refused before any device work."""
+    ref = os.path.join(oracle.REFERENCE_DIR, "openmp-threading")
+    if not os.path.exists(os.path.join(ref, "XSbench_header.h")):
+        pytest.skip("reference checkout not present")
+    from xsbench_gb300 import build as B
+    src = tmp_path / "drop_in.c"
+    src.write_text(DROP_IN)
+    exe = tmp_path / "drop_in"
+    subprocess.run(["gcc", "-std=gnu99", "-Wall", "-Werror", "-I", ref, "-I",
+                    os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", B.LIB_DIR,
+                    "-lxsgb", f"-Wl,-rpath,{B.LIB_DIR}"], check=True)
+    p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.split()[0] == "1"          # XS_ERR_INVALID_ARGUMENT
