@@ -150,3 +150,12 @@ def test_drop_in_binding_compiles_with_the_reference_header(tmp_path):
     p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stderr
     assert p.stdout.split()[0] == "1"          # XS_ERR_INVALID_ARGUMENT
+
+
+def test_e2e_breakdown_module_parses_its_arguments():
+    """The end-to-end breakdown diagnostic (python -m xsbench_gb300.e2e_breakdown)
+    answers --help without a GPU."""
+    import sys
+    p = subprocess.run([sys.executable, "-m", "xsbench_gb300.e2e_breakdown", "--help"],
+                       capture_output=True, text=True, timeout=120, cwd=ROOT)
+    assert p.returncode == 0 and "--kernel" in p.stdout
