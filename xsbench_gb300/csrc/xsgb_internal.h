@@ -109,7 +109,7 @@ struct xs_ctx {
     size_t device_bytes = 0;
     xsgb::Scratch s;
     // tuned defaults
-    int plain_tile = 1024;
+    int plain_tile = 1536;                    // unionized grid (2,048 on the others)
     int batched_buckets = 4096;
     int batched_blocks_per_sm = 4;            // in 256-thread blocks (threads per SM / 256)
     int plain_block = 256;                    // threads per block of the plain kernel
