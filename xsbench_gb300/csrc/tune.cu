@@ -229,7 +229,7 @@ extern "C" xs_status xs_autotune(xs_ctx *ctx, const char *cache_path, xs_run_opt
                 for (int lanes : {1, 2, 4}) {
                     ctx->fuel_lanes = lanes;
                     ctx->batched_fuel_lanes = lanes;
-                    for (int tile : {512, 1024, 1536, 2048}) {
+                    for (int tile : {512, 1024, 1536, 2048, 3072}) {
                         xs_run_opts o;
                         xs_run_opts_init(&o);
                         o.count = sample;
