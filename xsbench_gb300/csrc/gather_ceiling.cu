@@ -3,7 +3,7 @@
 // record (or bin record) per nuclide.
 //
 // Each warp reads 32 random 128-byte-aligned lines, one per lane (four 32-byte
-// loads each), all inside one window of 2^W bytes chosen at random per round:
+// loads each), all inside one window of 2^W bytes chosen at random per iteration:
 // the pattern of a warp of energy-sorted lookups reading one nuclide's
 // records, whose addresses spread over a window set by the warp's energy
 // range.  Windows from 64 KB to the whole buffer, then a streaming read of the
@@ -40,7 +40,7 @@ __device__ __forceinline__ unsigned long long ld32_xor(const char *p)
 // buffer of 2^buf_log2 bytes; every address stays below it: the window base
 // is (w << win_log2) with w < 2^(buf_log2 - win_log2), the line offset
 // (l << 7) + 96 + 32 with l < 2^(win_log2 - 7)
-__global__ void k_window_gather(const char *buf, int buf_log2, int win_log2, int rounds,
+__global__ void k_window_gather(const char *buf, int buf_log2, int win_log2, int iters,
                                 unsigned long long *out)
 {
     const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
@@ -49,7 +49,7 @@ __global__ void k_window_gather(const char *buf, int buf_log2, int win_log2, int
     const unsigned long long win_mask = (1ULL << (buf_log2 - win_log2)) - 1;
     const unsigned long long line_mask = (1ULL << (win_log2 - 7)) - 1;
     unsigned long long acc = 0;
-    for (int r = 0; r < rounds; r++) {
+    for (int r = 0; r < iters; r++) {
         const unsigned long long w = mix64(warp * 0x9E3779B97F4A7C15ULL + (unsigned)r) & win_mask;
         const unsigned long long l =
             mix64((warp << 20) ^ ((unsigned long long)r << 5) ^ lane ^ 0x5555ULL) & line_mask;
@@ -94,7 +94,7 @@ int main(int argc, char **argv)
     if (e != cudaSuccess) return fail("memset", e);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-    const int threads = 256, blocks = sms * 8, rounds = 256, reps = 5;
+    const int threads = 256, blocks = sms * 8, iters = 256, reps = 5;
     const size_t nthreads = (size_t)threads * blocks;
     e = cudaMalloc(&out, nthreads * 8);
     if (e != cudaSuccess) return fail("output", e);
@@ -106,15 +106,15 @@ int main(int argc, char **argv)
     bool first = true;
     for (int w : wins) {
         if (w > buf_log2) continue;
-        k_window_gather<<<blocks, threads>>>(buf, buf_log2, w, rounds, out);
+        k_window_gather<<<blocks, threads>>>(buf, buf_log2, w, iters, out);
         cudaEventRecord(a);
-        for (int i = 0; i < reps; i++) k_window_gather<<<blocks, threads>>>(buf, buf_log2, w, rounds, out);
+        for (int i = 0; i < reps; i++) k_window_gather<<<blocks, threads>>>(buf, buf_log2, w, iters, out);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, a, b);
         printf("%s{\"window_bytes\": %llu, \"gbs\": %.1f}", first ? "" : ", ", 1ULL << w,
-               (double)nthreads * rounds * 128 * reps / (ms * 1e-3) / 1e9);
+               (double)nthreads * iters * 128 * reps / (ms * 1e-3) / 1e9);
         first = false;
     }
     const size_t n = bytes / 16;
