@@ -375,12 +375,15 @@ xs_status build_derived_tables(xs_ctx *ctx)
     // with the in-tile energy order (the hash and nuclide grids) the plain
     // kernel runs best in tiles of 2,048 (XL, guided: 616 against 518 M
     // lookups/s at 1,024; large hash grid, its own search: 754 against 738 M)
-    // plain tiles: 2,048 lookups on the hash and nuclide grids; 3,072 on
-    // long grids (the XL problem), whose bin-record reads gain from the
-    // denser energy order of a bigger tile while four blocks still share an
-    // SM (XL, hash / nuclide grid: 660 / 704 M lookups/s at 2,048, 707 / 755 M
-    // at 3,072, 685 / 737 M at 3,584; 597 M at 4,096, three blocks per SM)
-    if (t.grid_type != XS_UNIONIZED) ctx->plain_tile = t.n_gp > 65536 ? 3072 : 2048;
+    // plain tiles: 2,048 lookups on the hash grid, 1,536 on the nuclide grid
+    // (large problem: 749 against 745 M lookups/s, 727 against 715 M end to
+    // end; the hash grid 752 against 745 M at 1,536), 3,072 on long grids
+    // (the XL problem), whose bin-record reads gain from the denser energy
+    // order of a bigger tile while four blocks still share an SM (XL, hash /
+    // nuclide grid: 660 / 704 M at 2,048, 707 / 755 M at 3,072, 685 / 737 M at
+    // 3,584; 597 M at 4,096, three blocks per SM)
+    if (t.grid_type != XS_UNIONIZED)
+        ctx->plain_tile = t.n_gp > 65536 ? 3072 : t.grid_type == XS_NUCLIDE ? 1536 : 2048;
     if (t.grid_type == XS_UNIONIZED) {
         s = ctx_alloc(ctx, &p, (size_t)t.n_union * 8);
         if (s != XS_OK) return s;
